@@ -1,0 +1,177 @@
+/*
+ * sphgrid.h -- C ABI of the GB300 (sm_103a) sphMapping deposition library
+ * (libsphgrid.so).
+ *
+ * It replaces the Julia deposition path of SPHtoGrid.jl v0.5.3:
+ *   sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=Rho; param, kernel,
+ *              reduce_image, return_both_maps, dimensions, calc_mean, ...)
+ *   src/cic_interpolation/cic_interpolation.jl:35-272
+ * and below it center_particles / filter_particles_in_image
+ * (filter_shift.jl:6-67), cic_mapping_2D (cic_2D.jl:103-244), cic_mapping_3D
+ * (cic_3D.jl:110-208) and reduce_image_2D/3D (reduce_image.jl:8-55).
+ * A Julia `ccall` shim keeping the sphMapping signature is in
+ * sphtogrid.jl_gb300/julia/SPHtoGridGB300.jl; a Python ctypes mirror in
+ * sphtogrid.jl_gb300/mapping.py.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (SPHG_OK = 0).  No exception
+ *    crosses the ABI; sphg_last_error() gives the message of the last failed
+ *    call on a context.
+ *  - Arrays keep the Julia layouts: Pos is 3 x N column-major (element (c, p)
+ *    at pos[p*pos_stride_p + c*pos_stride_c], strides in elements, so both the
+ *    Julia layout (1 per component, 3 per particle) and a structure of arrays
+ *    are accepted); Bin_Quant is N or Nq x N the same way.
+ *  - Outputs are Float64 in Julia's column-major layouts:
+ *      dimensions 2:                 (P, P, Nq) indexed [x, y, q]
+ *      dimensions 2, return_both_maps: (P^2, Nq+1), row i*P + j (x slowest),
+ *                                    columns Q_1..Q_Nq then the weight W
+ *      dimensions 3:                 (P, P, P) indexed [z, y, x]
+ *  - A context is bound to one CUDA device and is safe to share between host
+ *    threads (calls on one context are serialised).
+ */
+#ifndef SPHGRID_H
+#define SPHGRID_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHG_ABI_VERSION 1
+
+typedef enum sphg_status {
+  SPHG_OK = 0,
+  SPHG_ERR_CENTER_EXTENT = 1, /* parameters.jl:67  error("Giving a center position ...") */
+  SPHG_ERR_PIXELS = 2,        /* parameters.jl:98  error("Please specify pixelSideLength ...") */
+  SPHG_ERR_DIMS = 3,          /* dimensions not 2 or 3 (the reference returns `nothing`) */
+  SPHG_ERR_NONFINITE = 4,     /* non-finite pixel range of a mapped particle (the
+                                 reference's floor(Integer, x) throws InexactError,
+                                 cic_shared.jl:292-293) */
+  SPHG_ERR_NQ = 5,            /* 3D maps a single scalar quantity (cic_3D.jl:140) */
+  SPHG_ERR_ALLOC = 6,         /* device or host allocation failed */
+  SPHG_ERR_ARG = 7,           /* null pointer, bad dtype, bad stride, bad size */
+  SPHG_ERR_CUDA = 8,          /* CUDA runtime error (message in sphg_last_error) */
+  SPHG_ERR_TIMEOUT = 9,       /* a device work queue gave up waiting (bounded spin) */
+  SPHG_ERR_NO_DEVICE = 10,    /* no CUDA device / extension built for another arch */
+  SPHG_ERR_UNSUPPORTED = 11   /* option combination not implemented */
+} sphg_status;
+
+enum { SPHG_F32 = 0, SPHG_F64 = 1 };
+
+/* SPHKernels.jl kernel types (README.md:57-63 of the reference). */
+enum {
+  SPHG_KERNEL_CUBIC = 0,
+  SPHG_KERNEL_QUINTIC = 1,
+  SPHG_KERNEL_WENDLAND_C4 = 2,
+  SPHG_KERNEL_WENDLAND_C6 = 3,
+  SPHG_KERNEL_WENDLAND_C8 = 4
+};
+
+/* Arithmetic of the deposition. */
+enum {
+  SPHG_PREC_FP64 = 0, /* plain FP64: the reference's arithmetic, FP64 atomics */
+  SPHG_PREC_FP32C = 1 /* FP32 weights + compensated FP32 tile sums, FP64 image */
+};
+
+enum { SPHG_MEM_DEVICE = 0, SPHG_MEM_HOST = 1 };
+
+/* What sphg_map does with positions before mapping. */
+enum {
+  SPHG_CENTER_NONE = 0,      /* positions are already centred on 0 */
+  SPHG_CENTER_INPLACE = 1,   /* Pos[d,i] -= center[d] written back into the caller's
+                                array, as the reference does (filter_shift.jl:15) */
+  SPHG_CENTER_READONLY = 2   /* centre on the fly, leave the caller's array intact */
+};
+
+/* Field-for-field image of `mappingParameters` (parameters.jl:14-27). */
+typedef struct sphg_params {
+  double x_lim[2], y_lim[2], z_lim[2];
+  double center[3];
+  double halfsize[3];
+  double len2pix;
+  double pixelSideLength;
+  int64_t Npixels[3];
+  double boxsize;
+  int32_t periodic;
+  int32_t pad_;
+} sphg_params;
+
+typedef struct sphg_particles {
+  int64_t n;
+  int32_t pos_dtype;  /* SPHG_F32 / SPHG_F64 */
+  int32_t attr_dtype; /* dtype of hsml, mass, rho, weights and bin_q */
+  void *pos;          /* 3 x n (see conventions); written when centering INPLACE */
+  int64_t pos_stride_p, pos_stride_c;
+  const void *hsml, *mass, *rho, *weights; /* length n, contiguous */
+  const void *bin_q;                       /* n_q x n */
+  int32_t n_q;
+  int32_t pad_;
+  int64_t q_stride_p, q_stride_k;
+} sphg_particles;
+
+typedef struct sphg_options {
+  int32_t dimensions;       /* 2 or 3 */
+  int32_t kernel;           /* SPHG_KERNEL_* */
+  int32_t kernel_dim;       /* dimension of the SPHKernels object (2 or 3) */
+  int32_t reduce_image;     /* sphMapping `reduce_image` */
+  int32_t return_both_maps; /* sphMapping `return_both_maps` (2D) */
+  int32_t calc_mean;        /* sphMapping `calc_mean` (2D; 3D always false) */
+  int32_t precision;        /* SPHG_PREC_* */
+  int32_t deterministic;    /* 1: bitwise reproducible sums (FP32C only) */
+  int32_t center;           /* SPHG_CENTER_* */
+  int32_t filter;           /* 1: keep particles whose centre is in the box (the
+                               reference's filter); 0: map every particle */
+  int32_t memspace;         /* SPHG_MEM_*: where pos/attrs/out live */
+  int32_t reserved[5];      /* must be 0 */
+} sphg_options;
+
+typedef struct sphg_stats {
+  int64_t n_in;          /* particles passed in */
+  int64_t n_mapped;      /* particles deposited (filtered and q != 0 or calc_mean) */
+  int64_t deposits;      /* sum of integer footprints of mapped particles */
+  double grid_mass;      /* 3D mass diagnostic (cic_3D.jl:186) */
+  double particle_mass;  /* 3D: sum of mapped particle masses (cic_3D.jl:192) */
+  sphg_params centred;   /* parameters re-derived around centre 0 (filter_shift.jl:292) */
+} sphg_stats;
+
+typedef struct sphg_context sphg_context;
+
+/* ABI version compiled into the library (SPHG_ABI_VERSION). */
+int sphg_abi_version(void);
+
+/* Message of a status code. */
+const char *sphg_status_string(int status);
+
+/* Create / destroy a context on CUDA device `device`.  The context owns a
+ * grow-only device workspace and pinned staging buffers. */
+int sphg_context_create(int device, sphg_context **out);
+int sphg_context_destroy(sphg_context *ctx);
+
+/* Message of the last failed call on `ctx` (never NULL). */
+const char *sphg_last_error(const sphg_context *ctx);
+
+/* mappingParameters(T; x_lim, y_lim, z_lim, center, x_size, y_size, z_size,
+ * pixelSideLength, Npixels, boxsize) -- parameters.jl:44-125.  Arguments take
+ * the reference's sentinel defaults: -1 ("not given") for limits, centre,
+ * sizes, pixelSideLength and boxsize; 0 for Npixels.  Host only. */
+int sphg_mapping_parameters(const double x_lim[2], const double y_lim[2],
+                            const double z_lim[2], const double center[3],
+                            double x_size, double y_size, double z_size,
+                            double pixelSideLength, int64_t Npixels, double boxsize,
+                            sphg_params *out);
+
+/* Number of doubles sphg_map writes to `out` for these options. */
+int64_t sphg_output_len(const sphg_params *par, const sphg_options *opt, int32_t n_q);
+
+/* sphMapping (cic_interpolation.jl:35-272): centre, filter, deposit, reduce.
+ * `stream` is a cudaStream_t (NULL: the context's own stream).  The call
+ * returns after the result is complete in `out`.  `stats` may be NULL. */
+int sphg_map(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
+             const sphg_particles *parts, double *out, void *stream, sphg_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHGRID_H */

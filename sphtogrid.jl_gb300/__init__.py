@@ -1,0 +1,16 @@
+"""GB300 (sm_103a) implementation of SPHtoGrid.jl's ``sphMapping`` deposition
+path behind the reference's interface.
+
+Public names mirror the Julia package: ``mappingParameters``, ``sphMapping``
+and the SPHKernels kernel constructors ``Cubic``, ``Quintic``,
+``WendlandC4``, ``WendlandC6``, ``WendlandC8``.  All compute runs in
+``libsphgrid.so`` (CUDA); there is no CPU fallback.
+"""
+from ._lib import SPHtoGridError, Context, default_context  # noqa: F401
+from .parameters import (Cubic, MappingParameters, Quintic, SPHKernel, WendlandC4,  # noqa: F401
+                         WendlandC6, WendlandC8, kernel_from_name, mappingParameters)
+from .mapping import sphMapping  # noqa: F401
+
+__all__ = ["mappingParameters", "MappingParameters", "sphMapping", "Cubic", "Quintic",
+           "WendlandC4", "WendlandC6", "WendlandC8", "SPHKernel", "kernel_from_name",
+           "SPHtoGridError", "Context", "default_context"]

@@ -1,0 +1,426 @@
+// abi.cu -- host side of the C ABI declared in include/sphgrid.h: contexts,
+// the mappingParameters constructor, argument checks, staging of host arrays
+// and dispatch to the deposition kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/sphgrid.h"
+#include "common.cuh"
+#include "internal.h"
+
+struct sphg_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string last_error;
+  void* ws = nullptr;  // grow-only device workspace
+  size_t ws_size = 0;
+  sphg::DevStatus* d_status = nullptr;
+  sphg::DevStatus* h_status = nullptr;  // pinned
+};
+
+namespace {
+
+thread_local std::string g_error;  // errors raised before a context exists
+
+const char* kStatusText[] = {
+    "ok",
+    "Giving a center position requires extent in x, y and z direction.",
+    "Please specify pixelSideLength or number of pixels!",
+    "dimensions must be 2 or 3",
+    "non-finite pixel range of a mapped particle (InexactError in floor)",
+    "3D mapping takes exactly one scalar quantity",
+    "allocation failed",
+    "invalid argument",
+    "CUDA error",
+    "device work queue timed out",
+    "no usable CUDA device",
+    "unsupported option combination",
+};
+
+int fail(sphg_context* ctx, int status, const std::string& msg) {
+  std::string m = std::string(sphg_status_string(status)) + (msg.empty() ? "" : ": " + msg);
+  if (ctx) ctx->last_error = m;
+  else g_error = m;
+  return status;
+}
+
+int cuda_fail(sphg_context* ctx, cudaError_t e, const char* where) {
+  cudaGetLastError();
+  return fail(ctx, e == cudaErrorNoKernelImageForDevice ? SPHG_ERR_NO_DEVICE : SPHG_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);  \
+  } while (0)
+
+// Keeps the caller's current device around a call.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+int ensure_ws(sphg_context* ctx, size_t bytes, cudaStream_t s) {
+  if (bytes <= ctx->ws_size) return SPHG_OK;
+  if (ctx->ws) {
+    CK(cudaStreamSynchronize(s));
+    CK(cudaFree(ctx->ws));
+    ctx->ws = nullptr;
+    ctx->ws_size = 0;
+  }
+  size_t want = bytes + bytes / 4 + (1u << 20);
+  cudaError_t e = cudaMalloc(&ctx->ws, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&ctx->ws, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      ctx->ws = nullptr;
+      return fail(ctx, SPHG_ERR_ALLOC, "device workspace of " + std::to_string(bytes) + " bytes");
+    }
+    want = bytes;
+  }
+  ctx->ws_size = want;
+  return SPHG_OK;
+}
+
+// Bump allocator over the workspace (256-byte aligned slices).
+struct Carve {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return o;
+  }
+};
+
+size_t dtype_size(int dt) { return dt == SPHG_F32 ? 4 : 8; }
+
+bool valid_dtype(int dt) { return dt == SPHG_F32 || dt == SPHG_F64; }
+
+}  // namespace
+
+extern "C" {
+
+int sphg_abi_version(void) { return SPHG_ABI_VERSION; }
+
+const char* sphg_status_string(int status) {
+  if (status < 0 || status > SPHG_ERR_UNSUPPORTED) return "unknown status";
+  return kStatusText[status];
+}
+
+const char* sphg_last_error(const sphg_context* ctx) {
+  if (!ctx) return g_error.c_str();
+  return ctx->last_error.c_str();
+}
+
+int sphg_context_create(int device, sphg_context** out) {
+  if (!out) return fail(nullptr, SPHG_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(nullptr, SPHG_ERR_NO_DEVICE, e != cudaSuccess ? cudaGetErrorString(e) : "no device");
+  }
+  if (device < 0 || device >= count) return fail(nullptr, SPHG_ERR_ARG, "device index out of range");
+  DeviceGuard g(device);
+  sphg_context* ctx = new sphg_context();
+  ctx->device = device;
+  auto bail = [&](cudaError_t err, const char* where) {
+    int st = cuda_fail(nullptr, err, where);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    delete ctx;
+    return st;
+  };
+  if ((e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+    return bail(e, "cudaDeviceGetAttribute");
+  cudaFuncAttributes fa;
+  if ((e = sphg::probe_kernel_image(&fa)) != cudaSuccess) return bail(e, "kernel image for this device");
+  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "cudaStreamCreate");
+  if ((e = cudaMalloc(&ctx->d_status, sizeof(sphg::DevStatus))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = cudaMallocHost(&ctx->h_status, sizeof(sphg::DevStatus))) != cudaSuccess)
+    return bail(e, "cudaMallocHost");
+  *out = ctx;
+  return SPHG_OK;
+}
+
+int sphg_context_destroy(sphg_context* ctx) {
+  if (!ctx) return SPHG_OK;
+  {
+    DeviceGuard g(ctx->device);
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ws) cudaFree(ctx->ws);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return SPHG_OK;
+}
+
+// mappingParameters constructor, parameters.jl:44-125.
+int sphg_mapping_parameters(const double x_lim_in[2], const double y_lim_in[2], const double z_lim_in[2],
+                            const double center_in[3], double x_size, double y_size, double z_size,
+                            double pixelSideLength, int64_t Npixels, double boxsize, sphg_params* out) {
+  if (!x_lim_in || !y_lim_in || !z_lim_in || !center_in || !out)
+    return fail(nullptr, SPHG_ERR_ARG, "NULL argument");
+  double xl[2] = {x_lim_in[0], x_lim_in[1]}, yl[2] = {y_lim_in[0], y_lim_in[1]};
+  double zl[2] = {z_lim_in[0], z_lim_in[1]};
+  double c[3] = {center_in[0], center_in[1], center_in[2]};
+  const bool xl_def = xl[0] == -1.0 && xl[1] == -1.0;
+  const bool yl_def = yl[0] == -1.0 && yl[1] == -1.0;
+  const bool zl_def = zl[0] == -1.0 && zl[1] == -1.0;
+  const bool c_def = c[0] == -1.0 && c[1] == -1.0 && c[2] == -1.0;
+  if (xl_def && yl_def && zl_def) {  // limits from centre and sizes (:58-69)
+    if (!c_def && x_size != -1.0 && y_size != -1.0 && z_size != -1.0) {
+      xl[0] = c[0] - 0.5 * x_size; xl[1] = c[0] + 0.5 * x_size;
+      yl[0] = c[1] - 0.5 * y_size; yl[1] = c[1] + 0.5 * y_size;
+      zl[0] = c[2] - 0.5 * z_size; zl[1] = c[2] + 0.5 * z_size;
+    } else {
+      return fail(nullptr, SPHG_ERR_CENTER_EXTENT, "");
+    }
+  }
+  if (x_size == -1.0) x_size = xl[1] - xl[0];  // :72-80
+  if (y_size == -1.0) y_size = yl[1] - yl[0];
+  if (z_size == -1.0) z_size = zl[1] - zl[0];
+  if (c_def) {  // :82-86
+    c[0] = xl[0] + 0.5 * x_size;
+    c[1] = yl[0] + 0.5 * y_size;
+    c[2] = zl[0] + 0.5 * z_size;
+  }
+  double max_size = (std::isnan(x_size) || std::isnan(y_size)) ? NAN : (x_size > y_size ? x_size : y_size);
+  if (pixelSideLength == -1.0 && Npixels != 0) {  // :91-99
+    pixelSideLength = max_size / (double)Npixels;
+  } else if (pixelSideLength != -1.0 && Npixels == 0) {
+    double np = std::floor(max_size / pixelSideLength);
+    if (!(std::fabs(np) < 9.2e18)) return fail(nullptr, SPHG_ERR_ARG, "Npixels not representable");
+    Npixels = (int64_t)np;
+    pixelSideLength = max_size / (double)Npixels;
+  } else {
+    return fail(nullptr, SPHG_ERR_PIXELS, "");
+  }
+  std::memset(out, 0, sizeof(*out));
+  std::memcpy(out->x_lim, xl, sizeof(xl));
+  std::memcpy(out->y_lim, yl, sizeof(yl));
+  std::memcpy(out->z_lim, zl, sizeof(zl));
+  std::memcpy(out->center, c, sizeof(c));
+  out->halfsize[0] = 0.5 * x_size;  // :113
+  out->halfsize[1] = 0.5 * y_size;
+  out->halfsize[2] = 0.5 * z_size;
+  out->len2pix = 1.0 / pixelSideLength;  // :115
+  out->pixelSideLength = pixelSideLength;
+  out->Npixels[0] = out->Npixels[1] = out->Npixels[2] = Npixels;
+  out->boxsize = boxsize;
+  out->periodic = boxsize != -1.0 ? 1 : 0;
+  return SPHG_OK;
+}
+
+int64_t sphg_output_len(const sphg_params* par, const sphg_options* opt, int32_t n_q) {
+  if (!par || !opt) return -1;
+  const int64_t P = par->Npixels[0];
+  if (opt->dimensions == 2) return opt->return_both_maps ? P * P * (n_q + 1) : P * P * n_q;
+  if (opt->dimensions == 3) return P * P * P;
+  return -1;
+}
+
+int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
+             double* out, void* stream, sphg_stats* stats) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!par || !opt || !pt || !out) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
+  const int dims = opt->dimensions;
+  if (dims != 2 && dims != 3) return fail(ctx, SPHG_ERR_DIMS, "");
+  const int nq = pt->n_q;
+  if (nq < 1 || nq > sphg::kMaxQ) return fail(ctx, SPHG_ERR_ARG, "n_q must be in 1..16");
+  if (dims == 3 && nq != 1) return fail(ctx, SPHG_ERR_NQ, "");
+  if (opt->kernel < 0 || opt->kernel > 4) return fail(ctx, SPHG_ERR_ARG, "unknown kernel");
+  if (opt->kernel_dim != 2 && opt->kernel_dim != 3) return fail(ctx, SPHG_ERR_ARG, "kernel_dim must be 2 or 3");
+  if (opt->precision != SPHG_PREC_FP64 && opt->precision != SPHG_PREC_FP32C)
+    return fail(ctx, SPHG_ERR_ARG, "unknown precision");
+  if (opt->center < 0 || opt->center > 2) return fail(ctx, SPHG_ERR_ARG, "unknown center mode");
+  if (opt->memspace != SPHG_MEM_DEVICE && opt->memspace != SPHG_MEM_HOST)
+    return fail(ctx, SPHG_ERR_ARG, "unknown memspace");
+  for (int r = 0; r < 5; ++r)
+    if (opt->reserved[r]) return fail(ctx, SPHG_ERR_ARG, "reserved option fields must be 0");
+  if (!valid_dtype(pt->pos_dtype) || !valid_dtype(pt->attr_dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
+  const int64_t n = pt->n;
+  if (n < 0) return fail(ctx, SPHG_ERR_ARG, "negative particle count");
+  if (n > 0 && (!pt->pos || !pt->hsml || !pt->mass || !pt->rho || !pt->weights || !pt->bin_q))
+    return fail(ctx, SPHG_ERR_ARG, "NULL particle array");
+  if (pt->pos_stride_p < 0 || pt->pos_stride_c < 0 || pt->q_stride_p < 0 || pt->q_stride_k < 0)
+    return fail(ctx, SPHG_ERR_ARG, "negative stride");
+  const int64_t P = par->Npixels[0];
+  if (P < 1 || P > (int64_t)1 << 20 || (dims == 3 && P > 4096))
+    return fail(ctx, SPHG_ERR_ARG, "Npixels out of range");
+  const int64_t PD = dims == 2 ? P * P : P * P * P;
+  const int64_t out_len = sphg_output_len(par, opt, nq);
+
+  // centred parameters, re-derived as center_particles does (filter_shift.jl:288-294)
+  sphg_params cpar;
+  {
+    const double* cen = par->center;
+    const double xl[2] = {par->x_lim[0] - cen[0], par->x_lim[1] - cen[0]};
+    const double yl[2] = {par->y_lim[0] - cen[1], par->y_lim[1] - cen[1]};
+    const double zl[2] = {par->z_lim[0] - cen[2], par->z_lim[1] - cen[2]};
+    const double c0[3] = {0.0, 0.0, 0.0};
+    int64_t Pmax = par->Npixels[0];
+    if (par->Npixels[1] > Pmax) Pmax = par->Npixels[1];
+    if (par->Npixels[2] > Pmax) Pmax = par->Npixels[2];
+    int st = sphg_mapping_parameters(xl, yl, zl, c0, -1.0, -1.0, -1.0, -1.0, Pmax, par->boxsize, &cpar);
+    if (st) return fail(ctx, st, g_error);
+  }
+
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  const bool host = opt->memspace == SPHG_MEM_HOST;
+  const size_t psz = dtype_size(pt->pos_dtype), asz = dtype_size(pt->attr_dtype);
+  const int64_t pos_span = n > 0 ? (n - 1) * pt->pos_stride_p + 2 * pt->pos_stride_c + 1 : 0;
+  const int64_t q_span = n > 0 ? (n - 1) * pt->q_stride_p + (int64_t)(nq - 1) * pt->q_stride_k + 1 : 0;
+
+  // workspace layout
+  Carve cv;
+  size_t o_pos = 0, o_h = 0, o_m = 0, o_r = 0, o_w = 0, o_q = 0, o_out = 0;
+  if (host) {
+    o_pos = cv.take(pos_span * psz);
+    o_h = cv.take(n * asz);
+    o_m = cv.take(n * asz);
+    o_r = cv.take(n * asz);
+    o_w = cv.take(n * asz);
+    o_q = cv.take(q_span * asz);
+    o_out = cv.take(out_len * sizeof(double));
+  }
+  // accumulator: 2D raw maps accumulate straight into the output, 3D keeps Q
+  // in the output and only the weight channel in the workspace.
+  const bool acc_in_out = (dims == 2 && opt->return_both_maps) || dims == 3;
+  const size_t o_acc = cv.take((acc_in_out ? (dims == 3 ? PD : 0) : PD * (nq + 1)) * sizeof(double));
+  if (int st = ensure_ws(ctx, cv.off, s)) return st;
+  char* ws = (char*)ctx->ws;
+
+  sphg::DevParticles d;
+  d.n = n;
+  d.pos_dtype = pt->pos_dtype;
+  d.attr_dtype = pt->attr_dtype;
+  d.sp = pt->pos_stride_p;
+  d.sc = pt->pos_stride_c;
+  d.nq = nq;
+  d.qsp = pt->q_stride_p;
+  d.qsk = pt->q_stride_k;
+  double* dout = out;
+  if (host) {
+    d.pos = ws + o_pos;
+    d.hsml = ws + o_h;
+    d.mass = ws + o_m;
+    d.rho = ws + o_r;
+    d.w = ws + o_w;
+    d.q = ws + o_q;
+    dout = (double*)(ws + o_out);
+    if (n > 0) {
+      CK(cudaMemcpyAsync(ws + o_pos, pt->pos, pos_span * psz, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(ws + o_h, pt->hsml, n * asz, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(ws + o_m, pt->mass, n * asz, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(ws + o_r, pt->rho, n * asz, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(ws + o_w, pt->weights, n * asz, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(ws + o_q, pt->bin_q, q_span * asz, cudaMemcpyHostToDevice, s));
+    }
+  } else {
+    d.pos = pt->pos;
+    d.hsml = pt->hsml;
+    d.mass = pt->mass;
+    d.rho = pt->rho;
+    d.w = pt->weights;
+    d.q = pt->bin_q;
+  }
+  double* acc;  // (nq+1) channels of PD doubles
+  double* acc_w;
+  if (dims == 2 && opt->return_both_maps) {
+    acc = dout;
+    acc_w = dout + (int64_t)nq * PD;
+  } else if (dims == 3) {
+    acc = dout;
+    acc_w = (double*)(ws + o_acc);
+  } else {
+    acc = (double*)(ws + o_acc);
+    acc_w = acc + (int64_t)nq * PD;
+  }
+
+  sphg::DevMapParams mp;
+  for (int k = 0; k < 3; ++k) {
+    mp.cen[k] = par->center[k];
+    mp.lo[k] = cpar.center[k] - cpar.halfsize[k];
+    mp.hi[k] = cpar.center[k] + cpar.halfsize[k];
+  }
+  mp.boxsize = par->boxsize;
+  mp.periodic = par->periodic;
+  mp.center_mode = opt->center;
+  mp.filter = opt->filter;
+  mp.calc_mean = dims == 2 ? opt->calc_mean : 0;  // cic_mapping_3D gets no calc_mean (:219)
+  mp.kernel_dim = opt->kernel_dim;
+  mp.dims = dims;
+  mp.L = cpar.len2pix;
+  mp.P = P;
+  mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
+
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
+  if (dims == 3) {
+    CK(cudaMemsetAsync(acc, 0, PD * sizeof(double), s));
+    CK(cudaMemsetAsync(acc_w, 0, PD * sizeof(double), s));
+  } else {
+    CK(cudaMemsetAsync(acc, 0, PD * (nq + 1) * sizeof(double), s));
+  }
+
+  if (opt->precision == SPHG_PREC_FP64) {
+    sphg::launch_plain_fp64(opt->kernel, d, mp, acc, acc_w, PD, ctx->d_status, ctx->num_sms, s);
+  } else {
+    return fail(ctx, SPHG_ERR_UNSUPPORTED, "FP32C precision is not available in this build");
+  }
+  CK(cudaGetLastError());
+
+  if (dims == 2) {
+    if (!opt->return_both_maps) sphg::launch_reduce_2d(acc, P, nq, opt->reduce_image, dout, s);
+  } else {
+    sphg::launch_reduce_3d(acc, acc_w, PD, opt->reduce_image ? 0 : 1, dout, ctx->num_sms, s);
+  }
+  CK(cudaGetLastError());
+  if (host) {
+    CK(cudaMemcpyAsync(out, dout, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (opt->center == SPHG_CENTER_INPLACE && n > 0)
+      CK(cudaMemcpyAsync(pt->pos, d.pos, pos_span * psz, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const sphg::DevStatus hs = *ctx->h_status;
+  if (stats) {
+    stats->n_in = n;
+    stats->n_mapped = (int64_t)hs.n_mapped;
+    stats->deposits = (int64_t)hs.deposits;
+    stats->grid_mass = hs.grid_mass;
+    stats->particle_mass = hs.particle_mass;
+    stats->centred = cpar;
+  }
+  if (hs.flags & sphg::kFlagNonFinite) return fail(ctx, SPHG_ERR_NONFINITE, "");
+  if (hs.flags & sphg::kFlagTimeout) return fail(ctx, SPHG_ERR_TIMEOUT, "");
+  ctx->last_error.clear();
+  return SPHG_OK;
+}
+
+}  // extern "C"
