@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Benchmark of the sphMapping deposition on one GB300.
+
+Workload (default): the 3D gridded deposition -- N = 2^22 Float32 particles
+drawn as 64 Gaussian clumps plus a 20% uniform background in the unit cube,
+hsml from the local density, Bin_Quant = lognormal temperature, WendlandC6,
+256^3 grid, reduce_image = true.  A step is one ``sphg_map`` call over that
+map; ``value`` is particle-pixel deposits per second with the inputs already
+resident in HBM, ``e2e`` the same through the C ABI with pinned host buffers
+(host->device copies of the inputs and device->host copy of the map inside
+the timed region).
+
+``--impl reference`` times the CPU restatement of the reference's FP64
+algorithm (the oracle, all host threads, the reference's parallel=true
+decomposition) on the same workload and metric.
+
+With torchrun (N > 1) every rank maps its own copy of the workload on its own
+GPU (replicas: the path has no exchange step); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("particle-pixel deposits/s & maps/s: batched FP32-comp vs plain FP64 on GB300 "
+          "at ≤1e-5 rel err")
+WORKLOAD = ("3D gridded deposition: N=2^22 Float32 particles, 64 Gaussian clumps (sigma "
+            "0.02-0.08) + 20% uniform background, hsml from local density, Bin_Quant = "
+            "lognormal temperature, WendlandC6, 256^3 grid, reduce_image=true, seed 0")
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_workload(dtype=np.float32):
+    import __graft_entry__ as graft
+    pkg = graft.load_package()
+    from sphtogrid_gb300 import synth
+    return pkg, synth.clumps_3d(dtype=dtype)
+
+
+def oracle_module():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker: only the CPU-baseline leg runs it
+    oracle.build()
+    return oracle
+
+
+def run_oracle(O, d, frac=1.0, threads=None):
+    """One oracle map of (a contiguous fraction of) the workload; returns
+    (seconds, deposits, image)."""
+    n = d["pos"].shape[1]
+    m = max(1, int(round(n * frac)))
+    par = O.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["npix"])
+    threads = threads or os.cpu_count()
+    sl = slice(0, m)
+    pos = np.asfortranarray(d["pos"][:, sl])
+    t0 = time.perf_counter()
+    img, info = O.sph_mapping(pos, d["hsml"][sl], d["mass"][sl], d["rho"][sl], d["bin_q"][sl],
+                              d["weights"][sl], param=par, kernel=d["kernel"], dimensions=3,
+                              nthreads=threads, copy_pos=False)
+    dt = time.perf_counter() - t0
+    return dt, info["deposits"], img, threads, m
+
+
+def bench_reference(args):
+    """CPU restatement of the reference (the oracle) on the host cores."""
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    O = oracle_module()
+    _, d = load_workload()
+    # size each step to keep the whole run within a few minutes
+    t_est, _, _, threads, _ = run_oracle(O, d, frac=1.0 / 16)
+    per_step_budget = 150.0 / max(1, args.steps + args.warmup)
+    frac = min(1.0, per_step_budget / max(1e-3, 16 * t_est))
+    for _ in range(args.warmup):
+        run_oracle(O, d, frac=frac)
+    times, deps = [], 0
+    for _ in range(args.steps):
+        dt, dep, _, threads, m = run_oracle(O, d, frac=frac)
+        times.append(dt)
+        deps = dep
+    tot = sum(times)
+    value = deps * len(times) / tot
+    sample = (f"{m} of {d['pos'].shape[1]} particles (first {frac:.3f} of the shuffled set) "
+              f"mapped onto the full 256^3 grid per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "deposits/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "parallelism": f"cpu threads={threads}",
+                   "deposits_per_step": deps},
+        "cpu_baseline": {"value": value, "unit": "deposits/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "deposits/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _particles_struct(_lib, arrs, n, pos_dtype, attr_dtype, nq=1):
+    pt = _lib.SphgParticles()
+    pt.n = n
+    pt.pos_dtype = pos_dtype
+    pt.attr_dtype = attr_dtype
+    pt.pos, pt.hsml, pt.mass, pt.rho, pt.weights, pt.bin_q = arrs
+    pt.pos_stride_p, pt.pos_stride_c = 3, 1
+    pt.n_q = nq
+    pt.q_stride_p, pt.q_stride_k = 1, 0
+    return pt
+
+
+def bench_gpu(args):
+    import torch
+
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pkg, d = load_workload()
+    from sphtogrid_gb300 import _lib
+    L = _lib.lib()
+    ctx = pkg.default_context(local)
+    n = d["pos"].shape[1]
+    P = d["npix"]
+    par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+
+    def opts(prec, mem, profile=1):
+        o = _lib.SphgOptions()
+        o.dimensions = 3
+        o.kernel = pkg.WendlandC6(3).kind
+        o.kernel_dim = 3
+        o.reduce_image = 1
+        o.precision = _lib.PREC[prec]
+        o.center = _lib.CENTER_READONLY  # identical inputs every step
+        o.filter = 1
+        o.memspace = mem
+        o.profile = profile
+        return o
+
+    # device-resident inputs (Julia layout: xyz contiguous per particle)
+    t_pos = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).to(dev)
+    t_attr = [torch.from_numpy(np.ascontiguousarray(d[k])).to(dev)
+              for k in ("hsml", "mass", "rho", "weights", "bin_q")]
+    ptrs = [t_pos.data_ptr()] + [t.data_ptr() for t in t_attr]
+    pt_dev = _particles_struct(_lib, ptrs, n, _lib.SPHG_F32, _lib.SPHG_F32)
+    out_len = P ** 3
+    t_out = torch.empty(out_len, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def step(prec, st, pt=pt_dev, out=None, mem=_lib.MEM_DEVICE, profile=1):
+        o = opts(prec, mem, profile)
+        dst = C.c_void_p(t_out.data_ptr()) if out is None else out
+        _lib.check(L.sphg_map(ctx.handle, C.byref(par._c), C.byref(o), C.byref(pt), dst, sh,
+                              C.byref(st)), ctx.handle)
+
+    def timed(prec, steps, warmup):
+        st = _lib.SphgStats()
+        for _ in range(warmup):
+            step(prec, st)
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        phases = np.zeros(4)
+        launches = 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step(prec, st)
+            phases += np.array(list(st.phase_ms))
+            launches += st.n_launches
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+            dist.barrier()
+        return ms, st, phases / steps, launches
+
+    prec = args.precision
+    with ClockSampler(local) as clk:
+        ms, st, phases, launches = timed(prec, args.steps, args.warmup)
+    deposits = st.deposits
+    ms_step = ms / args.steps
+    value = deposits * args.steps * world / (ms * 1e-3)
+
+    # plain FP64 method on the same map (the speed-up denominator)
+    ms64, st64, ph64, _ = timed("fp64", max(2, args.steps // 4), 1)
+    img_fp64 = t_out.clone()
+    step(prec, _lib.SphgStats())
+    torch.cuda.synchronize(dev)
+    img_main = t_out.clone()
+    rel_vs_fp64 = _rel_linf(img_main.cpu().numpy(), img_fp64.cpu().numpy())
+
+    # end to end through the C ABI with pinned host buffers
+    h_pos = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).pin_memory()
+    h_attr = [torch.from_numpy(np.ascontiguousarray(d[k])).pin_memory()
+              for k in ("hsml", "mass", "rho", "weights", "bin_q")]
+    h_out = torch.empty(out_len, dtype=torch.float64).pin_memory()
+    pt_host = _particles_struct(_lib, [h_pos.data_ptr()] + [t.data_ptr() for t in h_attr], n,
+                                _lib.SPHG_F32, _lib.SPHG_F32)
+    e2e_steps = max(3, args.steps // 2)
+    ste = _lib.SphgStats()
+    for _ in range(2):
+        step(prec, ste, pt=pt_host, out=C.c_void_p(h_out.data_ptr()), mem=_lib.MEM_HOST, profile=0)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step(prec, ste, pt=pt_host, out=C.c_void_p(h_out.data_ptr()), mem=_lib.MEM_HOST, profile=0)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = h_pos.numel() * 4 + sum(t.numel() * t.element_size() for t in h_attr)
+    d2h = out_len * 8
+
+    # roofline of the dominant kernel (the tile deposit)
+    peaks = _peaks()
+    dep_ms = float(phases[2])
+    n_rec = st.n_mapped
+    dep_bytes = n_rec * (16 + 16 + 16 + 8 + 4) + out_len * 8
+    achieved = dep_bytes / (dep_ms * 1e-3) / 1e9 if dep_ms > 0 else None
+    traffic = _traffic_per_launch()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "deposits/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32" if prec == "fp32c" else "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": prec, "particles": n,
+                   "deposits_per_step": deposits, "maps_per_s": 1e3 / ms_step,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "working set (134 MB inputs + 60 B/particle records + 134 MB map) "
+                         "larger than the 129 MB L2; no flush"},
+        "phases_ms": {"prep": float(phases[0]), "norm": float(phases[1]),
+                      "deposit": float(phases[2]), "reduce": float(phases[3])},
+        "plain_fp64": {"ms_per_step": ms64 / max(2, args.steps // 4),
+                       "deposits_per_s": deposits * max(2, args.steps // 4) / (ms64 * 1e-3),
+                       "speedup_of_" + prec: (ms64 / max(2, args.steps // 4)) / ms_step,
+                       "rel_linf_" + prec + "_vs_fp64": rel_vs_fp64},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks[0], "unit": "GB/s",
+                     "frac": (achieved / peaks[0]) if achieved else None, "traffic": traffic,
+                     "kernel": "k_deposit", "peak_source": peaks[1],
+                     "algorithmic_bytes_per_launch": dep_bytes},
+        "e2e": {"value": deposits / e2e_s, "unit": "deposits/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        O = oracle_module()
+        dt, dep, img_ref, threads, m = run_oracle(O, d, frac=args.cpu_frac)
+        line["cpu_baseline"] = {
+            "value": dep / dt, "unit": "deposits/s", "cores": threads, "kind": "port",
+            "sample": (f"{m} of {n} particles mapped onto the full 256^3 grid by the FP64 "
+                       f"oracle, {threads} threads (parallel=true decomposition)")}
+        if m == n:
+            line["config"]["rel_linf_vs_oracle"] = _rel_linf(img_main.cpu().numpy(),
+                                                             np.asarray(img_ref).reshape(-1, order="F"))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def _rel_linf(a, b, floor=1e-9):
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    top = np.abs(b).max()
+    if top == 0:
+        return float(np.abs(a).max())
+    sel = np.abs(b) > floor * top
+    rel = np.abs(a[sel] - b[sel]) / np.abs(b[sel])
+    rest = np.abs(a[~sel] - b[~sel]).max() / top if (~sel).any() else 0.0
+    return float(max(rel.max() if rel.size else 0.0, rest))
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic_per_launch():
+    """DRAM bytes per deposit launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "deposit_traffic.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--cpu-frac", type=float, default=1.0,
+                    help="fraction of the particles the CPU baseline maps")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -123,8 +123,17 @@ typedef struct sphg_options {
   int32_t filter;           /* 1: keep particles whose centre is in the box (the
                                reference's filter); 0: map every particle */
   int32_t memspace;         /* SPHG_MEM_*: where pos/attrs/out live */
-  int32_t reserved[5];      /* must be 0 */
+  int32_t profile;          /* 1: time the phases with CUDA events (sphg_stats.phase_ms) */
+  int32_t reserved[4];      /* must be 0 */
 } sphg_options;
+
+/* Phases timed with sphg_options.profile (device time on the call's stream). */
+enum {
+  SPHG_PHASE_PREP = 0,    /* centring, filter, pixel ranges, tile counts */
+  SPHG_PHASE_NORM = 1,    /* renormalisation sums, tile lists */
+  SPHG_PHASE_DEPOSIT = 2, /* deposition (and, FP32C, the fused reduction) */
+  SPHG_PHASE_REDUCE = 3   /* separate Q/W reduction (FP64 path) */
+};
 
 typedef struct sphg_stats {
   int64_t n_in;          /* particles passed in */
@@ -133,6 +142,9 @@ typedef struct sphg_stats {
   double grid_mass;      /* 3D mass diagnostic (cic_3D.jl:186) */
   double particle_mass;  /* 3D: sum of mapped particle masses (cic_3D.jl:192) */
   sphg_params centred;   /* parameters re-derived around centre 0 (filter_shift.jl:292) */
+  int32_t n_launches;    /* kernels this call launched */
+  int32_t n_reruns;      /* FP32C: re-runs after growing the tile-pair list */
+  float phase_ms[4];     /* with profile: device milliseconds per SPHG_PHASE_* */
 } sphg_stats;
 
 typedef struct sphg_context sphg_context;

@@ -83,7 +83,8 @@ class SphgOptions(C.Structure):
         ("center", C.c_int32),
         ("filter", C.c_int32),
         ("memspace", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("profile", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -95,6 +96,9 @@ class SphgStats(C.Structure):
         ("grid_mass", C.c_double),
         ("particle_mass", C.c_double),
         ("centred", SphgParams),
+        ("n_launches", C.c_int32),
+        ("n_reruns", C.c_int32),
+        ("phase_ms", C.c_float * 4),
     ]
 
 

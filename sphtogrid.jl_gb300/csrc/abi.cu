@@ -23,6 +23,8 @@ struct sphg_context {
   size_t ws_size = 0;
   sphg::DevStatus* d_status = nullptr;
   sphg::DevStatus* h_status = nullptr;  // pinned
+  size_t pair_cap = 0;                  // FP32C tile-pair list capacity (grow-only)
+  cudaEvent_t ev[5] = {};               // phase timing events
 };
 
 namespace {
@@ -159,6 +161,8 @@ int sphg_context_create(int device, sphg_context** out) {
   if ((e = cudaMalloc(&ctx->d_status, sizeof(sphg::DevStatus))) != cudaSuccess) return bail(e, "cudaMalloc");
   if ((e = cudaMallocHost(&ctx->h_status, sizeof(sphg::DevStatus))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
+  for (int k = 0; k < 5; ++k)
+    if ((e = cudaEventCreate(&ctx->ev[k])) != cudaSuccess) return bail(e, "cudaEventCreate");
   *out = ctx;
   return SPHG_OK;
 }
@@ -172,6 +176,8 @@ int sphg_context_destroy(sphg_context* ctx) {
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    for (int k = 0; k < 5; ++k)
+      if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
   }
   delete ctx;
@@ -260,7 +266,7 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   if (opt->center < 0 || opt->center > 2) return fail(ctx, SPHG_ERR_ARG, "unknown center mode");
   if (opt->memspace != SPHG_MEM_DEVICE && opt->memspace != SPHG_MEM_HOST)
     return fail(ctx, SPHG_ERR_ARG, "unknown memspace");
-  for (int r = 0; r < 5; ++r)
+  for (int r = 0; r < 4; ++r)
     if (opt->reserved[r]) return fail(ctx, SPHG_ERR_ARG, "reserved option fields must be 0");
   if (!valid_dtype(pt->pos_dtype) || !valid_dtype(pt->attr_dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
   const int64_t n = pt->n;
@@ -293,10 +299,19 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   DeviceGuard g(ctx->device);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   const bool host = opt->memspace == SPHG_MEM_HOST;
+  const bool fp32c = opt->precision == SPHG_PREC_FP32C;
   const size_t psz = dtype_size(pt->pos_dtype), asz = dtype_size(pt->attr_dtype);
   const int64_t pos_span = n > 0 ? (n - 1) * pt->pos_stride_p + 2 * pt->pos_stride_c + 1 : 0;
   const int64_t q_span = n > 0 ? (n - 1) * pt->q_stride_p + (int64_t)(nq - 1) * pt->q_stride_k + 1 : 0;
 
+  sphg::TiledArgs ta;
+  std::memset(&ta, 0, sizeof(ta));
+  if (fp32c) sphg::tiled_geometry(dims, P, ta.tdim, ta.ntile, &ta.n_tiles);
+  int rerun = 0;
+  long long pair_cap = (long long)ctx->pair_cap;
+  if (fp32c && pair_cap < 8 * n + ta.n_tiles) pair_cap = 8 * n + ta.n_tiles;
+
+again:
   // workspace layout
   Carve cv;
   size_t o_pos = 0, o_h = 0, o_m = 0, o_r = 0, o_w = 0, o_q = 0, o_out = 0;
@@ -309,10 +324,27 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
     o_q = cv.take(q_span * asz);
     o_out = cv.take(out_len * sizeof(double));
   }
-  // accumulator: 2D raw maps accumulate straight into the output, 3D keeps Q
-  // in the output and only the weight channel in the workspace.
+  // FP64 path accumulator: 2D raw maps accumulate straight into the output,
+  // 3D keeps Q in the output and only the weight channel in the workspace.
   const bool acc_in_out = (dims == 2 && opt->return_both_maps) || dims == 3;
-  const size_t o_acc = cv.take((acc_in_out ? (dims == 3 ? PD : 0) : PD * (nq + 1)) * sizeof(double));
+  size_t o_acc = 0;
+  if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 ? PD : 0) : PD * (nq + 1)) * sizeof(double));
+  size_t o_box = 0, o_dim = 0, o_geo = 0, o_cp = 0, o_aux = 0, o_qv = 0, o_cnt = 0, o_start = 0,
+         o_pairs = 0, o_nrec = 0, o_exps = 0;
+  const int64_t cap = n > 0 ? n : 1;
+  if (fp32c) {
+    o_box = cv.take(cap * sizeof(int4));
+    o_dim = cv.take(cap * sizeof(int4));
+    o_geo = cv.take(cap * sizeof(float4));
+    o_cp = cv.take(cap * sizeof(double));
+    o_aux = cv.take(cap * sizeof(double));
+    o_qv = cv.take(cap * nq * sizeof(float));
+    o_cnt = cv.take((2 * ta.n_tiles + 1) * sizeof(int));  // counts, fill, record counter
+    o_start = cv.take((ta.n_tiles + 1) * sizeof(long long));
+    o_pairs = cv.take(pair_cap * sizeof(int));
+    o_nrec = o_cnt + 2 * ta.n_tiles * sizeof(int);
+    o_exps = cv.take((sphg::kMaxQ + 1) * sizeof(int));
+  }
   if (int st = ensure_ws(ctx, cv.off, s)) return st;
   char* ws = (char*)ctx->ws;
 
@@ -334,7 +366,7 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
     d.w = ws + o_w;
     d.q = ws + o_q;
     dout = (double*)(ws + o_out);
-    if (n > 0) {
+    if (n > 0 && rerun == 0) {
       CK(cudaMemcpyAsync(ws + o_pos, pt->pos, pos_span * psz, cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(ws + o_h, pt->hsml, n * asz, cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(ws + o_m, pt->mass, n * asz, cudaMemcpyHostToDevice, s));
@@ -350,18 +382,6 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
     d.w = pt->weights;
     d.q = pt->bin_q;
   }
-  double* acc;  // (nq+1) channels of PD doubles
-  double* acc_w;
-  if (dims == 2 && opt->return_both_maps) {
-    acc = dout;
-    acc_w = dout + (int64_t)nq * PD;
-  } else if (dims == 3) {
-    acc = dout;
-    acc_w = (double*)(ws + o_acc);
-  } else {
-    acc = (double*)(ws + o_acc);
-    acc_w = acc + (int64_t)nq * PD;
-  }
 
   sphg::DevMapParams mp;
   for (int k = 0; k < 3; ++k) {
@@ -372,6 +392,8 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   mp.boxsize = par->boxsize;
   mp.periodic = par->periodic;
   mp.center_mode = opt->center;
+  // a re-run after K1 already wrote centred positions back must not centre again
+  if (rerun && opt->center == SPHG_CENTER_INPLACE) mp.center_mode = SPHG_CENTER_NONE;
   mp.filter = opt->filter;
   mp.calc_mean = dims == 2 ? opt->calc_mean : 0;  // cic_mapping_3D gets no calc_mean (:219)
   mp.kernel_dim = opt->kernel_dim;
@@ -380,27 +402,73 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   mp.P = P;
   mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
 
+  cudaEvent_t* ev = opt->profile ? ctx->ev : nullptr;
+  int n_launch = 0;
   CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
-  if (dims == 3) {
-    CK(cudaMemsetAsync(acc, 0, PD * sizeof(double), s));
-    CK(cudaMemsetAsync(acc_w, 0, PD * sizeof(double), s));
-  } else {
-    CK(cudaMemsetAsync(acc, 0, PD * (nq + 1) * sizeof(double), s));
-  }
-
-  if (opt->precision == SPHG_PREC_FP64) {
+  if (!fp32c) {
+    double* acc;  // (nq+1) channels of PD doubles
+    double* acc_w;
+    if (dims == 2 && opt->return_both_maps) {
+      acc = dout;
+      acc_w = dout + (int64_t)nq * PD;
+    } else if (dims == 3) {
+      acc = dout;
+      acc_w = (double*)(ws + o_acc);
+    } else {
+      acc = (double*)(ws + o_acc);
+      acc_w = acc + (int64_t)nq * PD;
+    }
+    if (dims == 3) {
+      CK(cudaMemsetAsync(acc, 0, PD * sizeof(double), s));
+      CK(cudaMemsetAsync(acc_w, 0, PD * sizeof(double), s));
+    } else {
+      CK(cudaMemsetAsync(acc, 0, PD * (nq + 1) * sizeof(double), s));
+    }
+    if (ev) {
+      CK(cudaEventRecord(ev[0], s));
+      CK(cudaEventRecord(ev[1], s));
+      CK(cudaEventRecord(ev[2], s));
+    }
     sphg::launch_plain_fp64(opt->kernel, d, mp, acc, acc_w, PD, ctx->d_status, ctx->num_sms, s);
+    CK(cudaGetLastError());
+    if (ev) CK(cudaEventRecord(ev[3], s));
+    if (dims == 2) {
+      if (!opt->return_both_maps) sphg::launch_reduce_2d(acc, P, nq, opt->reduce_image, dout, s);
+    } else {
+      sphg::launch_reduce_3d(acc, acc_w, PD, opt->reduce_image ? 0 : 1, dout, ctx->num_sms, s);
+    }
+    CK(cudaGetLastError());
+    if (ev) CK(cudaEventRecord(ev[4], s));
+    n_launch = (dims == 2 && opt->return_both_maps) ? 1 : 2;
   } else {
-    return fail(ctx, SPHG_ERR_UNSUPPORTED, "FP32C precision is not available in this build");
+    ta.pt = d;
+    ta.mp = mp;
+    ta.mp_re = mp;
+    if (ta.mp_re.center_mode == SPHG_CENTER_INPLACE) ta.mp_re.center_mode = SPHG_CENTER_NONE;
+    ta.cap = cap;
+    ta.box = (int4*)(ws + o_box);
+    ta.dimv = (int4*)(ws + o_dim);
+    ta.geo = (float4*)(ws + o_geo);
+    ta.cp = (double*)(ws + o_cp);
+    ta.aux = (double*)(ws + o_aux);
+    ta.qv = (float*)(ws + o_qv);
+    ta.tile_count = (int*)(ws + o_cnt);
+    ta.tile_fill = ta.tile_count + ta.n_tiles;
+    ta.n_rec = (int*)(ws + o_nrec);
+    ta.tile_start = (long long*)(ws + o_start);
+    ta.pairs = (int*)(ws + o_pairs);
+    ta.pair_cap = pair_cap;
+    ta.exps = (int*)(ws + o_exps);
+    ta.st = ctx->d_status;
+    ta.out = dout;
+    ta.mode = dims == 3 ? 2 : (opt->return_both_maps ? 1 : 0);
+    ta.reduce = opt->reduce_image;
+    ta.w_is_one = opt->reduce_image ? 0 : 1;
+    CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 1) * sizeof(int), s));
+    CK(cudaMemsetAsync(ta.exps, 0x80, (sphg::kMaxQ + 1) * sizeof(int), s));
+    CK(sphg::launch_tiled_fp32(opt->kernel, ta, ctx->num_sms, s, ev, &n_launch));
+    if (ev) CK(cudaEventRecord(ev[4], s));
   }
-  CK(cudaGetLastError());
-
-  if (dims == 2) {
-    if (!opt->return_both_maps) sphg::launch_reduce_2d(acc, P, nq, opt->reduce_image, dout, s);
-  } else {
-    sphg::launch_reduce_3d(acc, acc_w, PD, opt->reduce_image ? 0 : 1, dout, ctx->num_sms, s);
-  }
-  CK(cudaGetLastError());
   if (host) {
     CK(cudaMemcpyAsync(out, dout, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (opt->center == SPHG_CENTER_INPLACE && n > 0)
@@ -409,6 +477,16 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const sphg::DevStatus hs = *ctx->h_status;
+  if (fp32c && (hs.flags & sphg::kFlagOverflow) && !(hs.flags & sphg::kFlagNonFinite)) {
+    // more (particle, tile) pairs than the list holds: grow it and map again
+    long long total = 0;
+    CK(cudaMemcpy(&total, ta.tile_start + ta.n_tiles, sizeof(long long), cudaMemcpyDeviceToHost));
+    pair_cap = total + total / 8 + 1024;
+    ctx->pair_cap = (size_t)pair_cap;
+    if (++rerun > 2) return fail(ctx, SPHG_ERR_ALLOC, "tile-pair list kept overflowing");
+    goto again;
+  }
+  if (fp32c && (size_t)pair_cap > ctx->pair_cap) ctx->pair_cap = (size_t)pair_cap;
   if (stats) {
     stats->n_in = n;
     stats->n_mapped = (int64_t)hs.n_mapped;
@@ -416,6 +494,11 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
     stats->grid_mass = hs.grid_mass;
     stats->particle_mass = hs.particle_mass;
     stats->centred = cpar;
+    stats->n_launches = n_launch;
+    stats->n_reruns = rerun;
+    for (int k = 0; k < 4; ++k) stats->phase_ms[k] = 0.0f;
+    if (ev)
+      for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&stats->phase_ms[k], ev[k], ev[k + 1]);
   }
   if (hs.flags & sphg::kFlagNonFinite) return fail(ctx, SPHG_ERR_NONFINITE, "");
   if (hs.flags & sphg::kFlagTimeout) return fail(ctx, SPHG_ERR_TIMEOUT, "");

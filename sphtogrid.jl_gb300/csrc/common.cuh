@@ -121,4 +121,118 @@ __device__ __forceinline__ bool floor_int(double v, int64_t* out) {
   return true;
 }
 
+// Julia min/max on finite floats.
+__device__ __forceinline__ double jmin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double jmax(double a, double b) { return b > a ? b : a; }
+
+// One particle after centring, filtering and unit conversion, in the
+// reference's FP64 arithmetic (translation units that include this header are
+// compiled without FMA contraction).
+struct PrepFP64 {
+  double x, y, z;           // pixel coordinates (get_xyz, cic_shared.jl:85-99)
+  double hsml, h_inv, knorm;
+  double area, col, vol;    // 2D: (2h)^2 and m/rho_pix/area; 3D: m/rho_pix
+  double m_in, rho_in, wgt;
+  int64_t lo[3], hi[3];     // pix_index_min_max per axis (hi = lo - 1 when empty)
+  bool scalar_zero;
+};
+
+enum { kPrepSkip = 0, kPrepMapped = 1, kPrepNonFinite = 2 };
+
+// center_particles / filter (filter_shift.jl:6-58), the quantity skip
+// (cic_2D.jl:154-168), get_quantities_2D/3D (cic_2D.jl:80-91,
+// cic_3D.jl:87-97), get_xyz and pix_index_min_max (cic_shared.jl:46-99).
+// `store_pos` writes the centred position back (SPHG_CENTER_INPLACE).
+template <int DIMS>
+__device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const DevMapParams& mp, int64_t p,
+                                                  bool store_pos, PrepFP64* o) {
+  double c[3];
+  bool in = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int64_t off = p * pt.sp + d * pt.sc;
+    double v = ld_elem(pt.pos_dtype, pt.pos, off);
+    if (mp.center_mode != 0) {
+      v = round_to(pt.pos_dtype, v - mp.cen[d]);
+      if (mp.periodic && fabs(v) > mp.boxsize / 2)
+        v = round_to(pt.pos_dtype, v > 0 ? v - mp.boxsize / 2 : v + mp.boxsize / 2);
+      if (mp.center_mode == 1 && store_pos) st_elem(pt.pos_dtype, pt.pos, off, v);
+    }
+    c[d] = v;
+    if (mp.filter && !(mp.lo[d] <= v && v <= mp.hi[d])) in = false;
+  }
+  if (!in) return kPrepSkip;
+  bool allzero = true;
+  for (int k = 0; k < pt.nq; ++k)
+    if (ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) != 0.0) allzero = false;
+  if (allzero && !mp.calc_mean) return kPrepSkip;
+  o->scalar_zero = (pt.nq > 1) && allzero;
+  const double L = mp.L;
+  const int64_t P = mp.P;
+  o->m_in = ld_elem(pt.attr_dtype, pt.mass, p);
+  o->rho_in = ld_elem(pt.attr_dtype, pt.rho, p);
+  o->wgt = ld_elem(pt.attr_dtype, pt.w, p);
+  const double hsml = ld_elem(pt.attr_dtype, pt.hsml, p) * L;
+  o->hsml = hsml;
+  o->h_inv = 1.0 / hsml;
+  o->area = o->col = o->vol = 0.0;
+  if (DIMS == 2) {
+    o->area = (2.0 * hsml) * (2.0 * hsml);
+    const double rho = o->rho_in * (1.0 / (L * L * L));
+    o->col = o->m_in / rho / o->area;
+  } else {
+    const double rho = o->rho_in / (L * L * L);
+    o->vol = o->m_in / rho;
+  }
+  const double hd = mp.kernel_dim == 2 ? o->h_inv * o->h_inv : o->h_inv * o->h_inv * o->h_inv;
+  o->knorm = mp.sigma * hd;
+  double x = c[0] * L, y = c[1] * L, z = c[2] * L;
+  x += 0.5 * (double)P;
+  y += 0.5 * (double)P;
+  z += 0.5 * (double)P;
+  o->x = x;
+  o->y = y;
+  o->z = z;
+  const double xs[3] = {x, y, z};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (d >= DIMS) {
+      o->lo[d] = 0;
+      o->hi[d] = 0;
+      continue;
+    }
+    int64_t a, b;
+    if (!floor_int(xs[d] - hsml, &a) || !floor_int(xs[d] + hsml, &b)) return kPrepNonFinite;
+    o->lo[d] = a > 0 ? a : 0;
+    o->hi[d] = b < P - 1 ? b : P - 1;
+    if (o->hi[d] < o->lo[d]) o->hi[d] = o->lo[d] - 1;
+  }
+  return kPrepMapped;
+}
+
+// Offset of a pixel centre and the overlap of [x - h, x + h] with pixel i
+// (get_x_dx / get_dxyz, cic_shared.jl:60-76).
+__device__ __forceinline__ void cell_axis_fp64(double x, double h, int64_t i, double* dist, double* ov) {
+  *dist = x - (double)i - 0.5;
+  *ov = jmin(x + h, (double)(i + 1)) - jmax(x - h, (double)i);
+}
+
+// Distance u (in units of h) and area/volume overlap of one footprint cell
+// (calculate_weights, cic_2D.jl:25-47, cic_3D.jl:28-53).
+template <int DIMS>
+__device__ __forceinline__ void cell_fp64(const PrepFP64& q, int64_t i, int64_t j, int64_t k, double* u, double* a) {
+  double xd, dx, yd, dy;
+  cell_axis_fp64(q.x, q.hsml, i, &xd, &dx);
+  cell_axis_fp64(q.y, q.hsml, j, &yd, &dy);
+  if (DIMS == 2) {
+    *u = sqrt(xd * xd + yd * yd) * q.h_inv;
+    *a = dx * dy;
+  } else {
+    double zd, dz;
+    cell_axis_fp64(q.z, q.hsml, k, &zd, &dz);
+    *a = dx * dy * dz;
+    *u = sqrt(xd * xd + yd * yd + zd * zd) * q.h_inv;
+  }
+}
+
 }  // namespace sphg

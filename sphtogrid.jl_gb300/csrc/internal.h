@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "tiled.cuh"
 
 namespace sphg {
 
@@ -19,5 +20,10 @@ void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& m
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s);
 void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one, double* out,
                       int num_sms, cudaStream_t s);
+
+// Tile shape and tile counts of the FP32-compensated path.
+void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles);
+cudaError_t launch_tiled_fp32(int kernel, const TiledArgs& A, int num_sms, cudaStream_t s,
+                              cudaEvent_t* ev, int* n_launch);
 
 }  // namespace sphg

@@ -25,16 +25,6 @@ __device__ __forceinline__ long long warp_sum(long long v) {
   return v;
 }
 
-// Julia min/max on finite floats.
-__device__ __forceinline__ double jmin(double a, double b) { return b < a ? b : a; }
-__device__ __forceinline__ double jmax(double a, double b) { return b > a ? b : a; }
-
-// Per-pixel geometry of one footprint cell: pixel-centre offsets and overlap.
-__device__ __forceinline__ void cell_axis(double x, double h, int64_t i, double* dist, double* ov) {
-  *dist = x - (double)i - 0.5;                                   // get_x_dx, cic_shared.jl:70-76
-  *ov = jmin(x + h, (double)(i + 1)) - jmax(x - h, (double)i);   // get_dxyz, cic_shared.jl:60-62
-}
-
 // One warp deposits one particle: pass 1 sums kernel x area weights over the
 // footprint (calculate_weights), pass 2 recomputes them and adds the
 // renormalised weight to the image (update_image!).
@@ -53,65 +43,12 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
   unsigned flags = 0;
 
   for (int64_t p = wid; p < pt.n; p += nw) {
-    // center_particles (filter_shift.jl:6-32) and filter (filter_shift.jl:40-58)
-    double c[3];
-    bool in = true;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int64_t o = p * pt.sp + d * pt.sc;
-      double v = ld_elem(pt.pos_dtype, pt.pos, o);
-      if (mp.center_mode != 0) {
-        v = round_to(pt.pos_dtype, v - mp.cen[d]);
-        if (mp.periodic && fabs(v) > mp.boxsize / 2)
-          v = round_to(pt.pos_dtype, v > 0 ? v - mp.boxsize / 2 : v + mp.boxsize / 2);
-        if (mp.center_mode == 1 && lane == 0) st_elem(pt.pos_dtype, pt.pos, o, v);
-      }
-      c[d] = v;
-      if (mp.filter && !(mp.lo[d] <= v && v <= mp.hi[d])) in = false;
-    }
-    if (!in) continue;
-    // skip particles without a quantity (cic_2D.jl:154-168, cic_3D.jl:140-144)
-    bool allzero = true;
-    for (int k = 0; k < nq; ++k)
-      if (ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) != 0.0) allzero = false;
-    if (allzero && !mp.calc_mean) continue;
-    const bool scalar_zero = (nq > 1) && allzero;
-
-    const double m_in = ld_elem(pt.attr_dtype, pt.mass, p);
-    const double rho_in = ld_elem(pt.attr_dtype, pt.rho, p);
-    const double wgt = ld_elem(pt.attr_dtype, pt.w, p);
-    const double hsml = ld_elem(pt.attr_dtype, pt.hsml, p) * L;
-    const double h_inv = 1.0 / hsml;
-    double area = 0.0, col = 0.0, vol = 0.0;
-    if (DIMS == 2) {  // get_quantities_2D, cic_2D.jl:80-91
-      area = (2.0 * hsml) * (2.0 * hsml);
-      const double rho = rho_in * (1.0 / (L * L * L));
-      col = m_in / rho / area;
-    } else {  // get_quantities_3D, cic_3D.jl:87-97
-      const double rho = rho_in / (L * L * L);
-      vol = m_in / rho;
-    }
-    const double hd = mp.kernel_dim == 2 ? h_inv * h_inv : h_inv * h_inv * h_inv;
-    const double knorm = mp.sigma * hd;  // SPHKernels normalisation x h_inv^D
-    // get_xyz (cic_shared.jl:85-99) and pix_index_min_max (cic_shared.jl:46-52)
-    double x = c[0] * L, y = c[1] * L, z = c[2] * L;
-    x += 0.5 * (double)P;
-    y += 0.5 * (double)P;
-    z += 0.5 * (double)P;
-    int64_t a0, a1, b0, b1, e0 = 0, e1 = 0;
-    if (!floor_int(x - hsml, &a0) || !floor_int(x + hsml, &a1) || !floor_int(y - hsml, &b0) ||
-        !floor_int(y + hsml, &b1) ||
-        (DIMS == 3 && (!floor_int(z - hsml, &e0) || !floor_int(z + hsml, &e1)))) {
-      flags |= kFlagNonFinite;
-      continue;
-    }
-    const int64_t iMin = a0 > 0 ? a0 : 0, iMax = a1 < P - 1 ? a1 : P - 1;
-    const int64_t jMin = b0 > 0 ? b0 : 0, jMax = b1 < P - 1 ? b1 : P - 1;
-    const int64_t kMin = DIMS == 3 ? (e0 > 0 ? e0 : 0) : 0;
-    const int64_t kMax = DIMS == 3 ? (e1 < P - 1 ? e1 : P - 1) : 0;
-    const int64_t ni = iMax >= iMin ? iMax - iMin + 1 : 0;
-    const int64_t nj = jMax >= jMin ? jMax - jMin + 1 : 0;
-    const int64_t nk = kMax >= kMin ? kMax - kMin + 1 : 0;
+    PrepFP64 q;
+    const int state = prep_particle_fp64<DIMS>(pt, mp, p, lane == 0, &q);
+    if (state == kPrepNonFinite) flags |= kFlagNonFinite;
+    if (state != kPrepMapped) continue;
+    const int64_t iMin = q.lo[0], jMin = q.lo[1], kMin = q.lo[2];
+    const int64_t ni = q.hi[0] - iMin + 1, nj = q.hi[1] - jMin + 1, nk = q.hi[2] - kMin + 1;
     const int64_t njk = nj * nk;
     const int64_t F = ni * njk;
 
@@ -121,22 +58,12 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
     for (int64_t f = lane; f < F; f += 32) {
       const int64_t ia = f / njk, r = f - ia * njk;
       const int64_t jb = r / nk, kc = r - jb * nk;
-      double xd, dx, yd, dy, zd = 0.0, dz = 1.0;
-      cell_axis(x, hsml, iMin + ia, &xd, &dx);
-      cell_axis(y, hsml, jMin + jb, &yd, &dy);
       double u, a;
-      if (DIMS == 2) {
-        u = sqrt(xd * xd + yd * yd) * h_inv;
-        a = dx * dy;
-      } else {
-        cell_axis(z, hsml, kMin + kc, &zd, &dz);
-        a = dx * dy * dz;
-        u = sqrt(xd * xd + yd * yd + zd * zd) * h_inv;
-      }
+      cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &u, &a);
       s_a += a;
       n_t += 1;
       if (u <= 1.0) {
-        s_w += kshape<KERN, double>(u) * knorm * a;
+        s_w += kshape<KERN, double>(u) * q.knorm * a;
         n_d += 1;
       }
     }
@@ -152,8 +79,8 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
     } else {
       wpp = (double)n_d / s_w;
     }
-    const double norm = DIMS == 2 ? area / (double)n_d * wpp * wgt * col
-                                  : vol / (double)n_d * wpp * wgt * L;
+    const double norm = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                                  : q.vol / (double)n_d * wpp * q.wgt * L;
 
     // pass 2: deposit (cic_2D.jl:193-222, cic_3D.jl:172-188)
     double gm = 0.0;
@@ -161,37 +88,27 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
       const int64_t ia = f / njk, r = f - ia * njk;
       const int64_t jb = r / nk, kc = r - jb * nk;
       const int64_t i = iMin + ia, j = jMin + jb, k = kMin + kc;
-      double xd, dx, yd, dy, zd = 0.0, dz = 1.0;
-      cell_axis(x, hsml, i, &xd, &dx);
-      cell_axis(y, hsml, j, &yd, &dy);
       double u, a;
-      if (DIMS == 2) {
-        u = sqrt(xd * xd + yd * yd) * h_inv;
-        a = dx * dy;
-      } else {
-        cell_axis(z, hsml, k, &zd, &dz);
-        a = dx * dy * dz;
-        u = sqrt(xd * xd + yd * yd + zd * zd) * h_inv;
-      }
-      const double wk = fallback ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * knorm : 0.0);
+      cell_fp64<DIMS>(q, i, j, k, &u, &a);
+      const double wk = fallback ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * q.knorm : 0.0);
       const double pw = wk * a * norm;
       const int64_t idx = DIMS == 2 ? i * P + j : (i * P + j) * P + k;
       if (pw != 0.0) {
         atomicAdd(accw + idx, pw);
-        if (scalar_zero) {
+        if (q.scalar_zero) {
           atomicAdd(accq + idx, 0.0 * pw);
         } else {
-          for (int q = 0; q < nq; ++q)
-            atomicAdd(accq + idx + q * PD, ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + q * pt.qsk) * pw);
+          for (int c = 0; c < nq; ++c)
+            atomicAdd(accq + idx + c * PD, ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + c * pt.qsk) * pw);
         }
       }
-      if (DIMS == 3) gm += rho_in * wk * a / (L * L * L);
+      if (DIMS == 3) gm += q.rho_in * wk * a / (L * L * L);
     }
     c_gm += gm;
     if (lane == 0) {
       c_mapped += 1;
       c_dep += (unsigned long long)F;
-      c_pm += m_in;
+      c_pm += q.m_in;
     }
   }
   // fold the per-thread statistics: one atomic per warp

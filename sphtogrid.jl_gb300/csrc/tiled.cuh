@@ -1,0 +1,137 @@
+// tiled.cuh -- the FP32-compensated, image-tiled deposition.
+//
+// Pipeline for one map (all on one stream):
+//   K1 k_prep_count   one thread per input particle: centring, filter, quantity
+//                     skip and FP64 pixel ranges exactly as the reference
+//                     (prep_particle_fp64); compacts mapped particles into
+//                     records with FP32 local coordinates and counts the
+//                     (particle, tile) overlaps per image tile.
+//   K2 k_scan_tiles   exclusive scan of the tile counts (one CTA).
+//   K3 k_norm_fill    one warp per record: the renormalisation sum
+//                     S = sum(w(u) A) over the whole footprint (calculate_weights,
+//                     cic_2D.jl:11-72) in FP32 with compensated lane sums; tiny,
+//                     ill-conditioned particles (no pixel centre well inside the
+//                     kernel) are redone in the reference's FP64 arithmetic.
+//                     Writes each record's index into the lists of its tiles.
+//   K4 k_deposit      one CTA per image tile: every (particle, tile) pair adds
+//                     w(u) A c_p (and q times it) to shared-memory accumulators
+//                     with TwoSum-compensated FP32 atomics; the tile is then
+//                     flushed once, in FP64, straight into the output layout
+//                     (reduce_image_2D/3D fused: reduce_image.jl:8-55).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace sphg {
+
+enum : int { kRecFP64 = 1, kRecFallback = 2 };
+
+// Scale exponent target: the largest per-cell contribution of a channel is
+// brought to about 2^kScaleTop before it enters FP32 accumulators.
+constexpr int kScaleTop = 24;
+
+struct TiledArgs {
+  DevParticles pt;
+  DevMapParams mp;
+  DevMapParams mp_re;  // re-derivation after K1 (positions already centred in place)
+  int tdim[3];      // tile extent per axis (1 on the unused 2D axis)
+  int ntile[3];     // tiles per axis
+  int64_t n_tiles;
+  int64_t cap;      // record capacity
+  int* n_rec;       // number of records (device counter)
+  int4* box;        // {iMin, jMin, kMin, flags}
+  int4* dimv;       // {ni, nj, nk, source particle}
+  float4* geo;      // {x - iMin, y - jMin, z - kMin, h} in pixel units
+  double* cp;       // K1: numerator of the weight factor; K3: the factor
+  double* aux;      // rho / L^3 * kernel normalisation (3D mass diagnostic)
+  float* qv;        // quantities, qv[k * cap + r]
+  int* tile_count;  // per tile, zeroed before K1
+  int* tile_fill;   // per tile, zeroed before K3
+  long long* tile_start;  // n_tiles + 1
+  int* pairs;
+  long long pair_cap;
+  int* exps;        // per channel max exponent (channels 0..nq-1 = Q, nq = W)
+  DevStatus* st;
+  // output
+  double* out;
+  int mode;         // 0: 2D reduced, 1: 2D raw accumulator, 2: 3D reduced
+  int reduce;       // 2D reduce_image
+  int w_is_one;     // 3D !reduce_image
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Error-free sum of two floats (Knuth's TwoSum): a + b == s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// Compensated accumulation into a shared-memory (hi, lo) pair: the atomic add
+// returns the value it added to, so the rounding error of that very addition
+// is recovered exactly with TwoSum and accumulated in `lo`.
+__device__ __forceinline__ void acc_twosum(float* hi, float* lo, float v) {
+  const float old = atomicAdd(hi, v);
+  float s, e;
+  two_sum(old, v, s, e);
+  if (e != 0.0f) atomicAdd(lo, e);
+}
+
+// FP32 kernel shape (no normalisation) via fused multiply-adds.
+template <int KERN>
+__device__ __forceinline__ float kshape_f(float u) {
+  if (KERN == 0) {
+    if (u < 0.5f) return fmaf(6.0f * (u - 1.0f), u * u, 1.0f);
+    const float t = 1.0f - u;
+    return 2.0f * t * t * t;
+  } else if (KERN == 1) {
+    const float a = 1.0f - u, b = (2.0f / 3.0f) - u, c = (1.0f / 3.0f) - u;
+    const float a2 = a * a, b2 = b * b, c2 = c * c;
+    const float a5 = a2 * a2 * a, b5 = b2 * b2 * b, c5 = c2 * c2 * c;
+    if (u < 1.0f / 3.0f) return fmaf(15.0f, c5, fmaf(-6.0f, b5, a5));
+    if (u < 2.0f / 3.0f) return fmaf(-6.0f, b5, a5);
+    return a5;
+  } else if (KERN == 2) {
+    const float t = 1.0f - u, t2 = t * t;
+    return t2 * t2 * t2 * fmaf(u, fmaf(35.0f / 3.0f, u, 6.0f), 1.0f);
+  } else if (KERN == 3) {
+    const float t = 1.0f - u, t2 = t * t, t4 = t2 * t2;
+    return t4 * t4 * fmaf(u, fmaf(u, fmaf(32.0f, u, 25.0f), 8.0f), 1.0f);
+  } else {
+    const float t = 1.0f - u, t2 = t * t, t4 = t2 * t2;
+    return t4 * t4 * t2 * fmaf(u, fmaf(u, fmaf(u, fmaf(429.0f / 5.0f, u, 90.0f), 42.0f), 10.0f), 1.0f);
+  }
+}
+
+// Overlap of [f - h, f + h] with local pixel a and the pixel-centre offset.
+__device__ __forceinline__ void axis_f(float f, float h, int a, float* dist, float* ov) {
+  const float fa = (float)a;
+  *dist = f - fa - 0.5f;
+  *ov = fminf(f + h, fa + 1.0f) - fmaxf(f - h, fa);
+}
+
+// Divide small non-negative integers with a float reciprocal (exact for
+// e < 2^22 and d <= 2^10 with the +0.5 guard).
+__device__ __forceinline__ int fdiv(int e, float inv_d) { return __float2int_rz(((float)e + 0.5f) * inv_d); }
+
+}  // namespace sphg

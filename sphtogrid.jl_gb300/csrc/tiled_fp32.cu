@@ -1,0 +1,461 @@
+// tiled_fp32.cu -- kernels and host launcher of the FP32-compensated tiled
+// deposition (see tiled.cuh for the pipeline).  Compiled with --fmad=false so
+// that the FP64 arithmetic shared with the plain path rounds exactly as the
+// reference; the FP32 hot loops use explicit fmaf.
+#include <cuda_runtime.h>
+
+#include <climits>
+
+#include "internal.h"
+#include "tiled.cuh"
+
+namespace sphg {
+
+namespace {
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// K1: one thread per input particle.
+template <int DIMS>
+__global__ void __launch_bounds__(256) k_prep_count(TiledArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long c_mapped = 0, c_dep = 0;
+  double c_pm = 0.0;
+  unsigned flags = 0;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < A.pt.n; base += stride) {
+    const int64_t p = base + threadIdx.x;
+    PrepFP64 q;
+    int state = kPrepSkip;
+    if (p < A.pt.n) state = prep_particle_fp64<DIMS>(A.pt, A.mp, p, true, &q);
+    if (state == kPrepNonFinite) flags |= kFlagNonFinite;
+    int ni = 0, nj = 0, nk = 0;
+    if (state == kPrepMapped) {
+      ni = (int)(q.hi[0] - q.lo[0] + 1);
+      nj = (int)(q.hi[1] - q.lo[1] + 1);
+      nk = (int)(q.hi[2] - q.lo[2] + 1);
+      c_mapped += 1;
+      c_dep += (unsigned long long)ni * nj * nk;
+      c_pm += q.m_in;
+    }
+    const bool rec = state == kPrepMapped && ni > 0 && nj > 0 && nk > 0;
+    // warp-aggregated slot allocation
+    const unsigned bal = __ballot_sync(0xffffffffu, rec);
+    int slot0 = 0;
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      if (lane == leader) slot0 = atomicAdd(A.n_rec, __popc(bal));
+      slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    }
+    if (rec) {
+      const int r = slot0 + __popc(bal & lanemask_lt());
+      const int i0 = (int)q.lo[0], j0 = (int)q.lo[1], k0 = (int)q.lo[2];
+      A.box[r] = make_int4(i0, j0, k0, 0);
+      A.dimv[r] = make_int4(ni, nj, nk, (int)p);
+      A.geo[r] = make_float4(__double2float_rn(q.x - (double)i0), __double2float_rn(q.y - (double)j0),
+                             DIMS == 3 ? __double2float_rn(q.z - (double)k0) : 0.0f,
+                             __double2float_rn(q.hsml));
+      // weight factor numerator: area*w*dz (cic_2D.jl:187-188) / vol*w*L (cic_3D.jl:168-169)
+      A.cp[r] = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
+      A.aux[r] = q.rho_in * q.knorm / (A.mp.L * A.mp.L * A.mp.L);
+      for (int k = 0; k < A.pt.nq; ++k)
+        A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
+            : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
+      // (particle, tile) overlaps
+      const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
+      const int ty0 = j0 / A.tdim[1], ty1 = (j0 + nj - 1) / A.tdim[1];
+      const int tz0 = k0 / A.tdim[2], tz1 = (k0 + nk - 1) / A.tdim[2];
+      for (int tx = tx0; tx <= tx1; ++tx)
+        for (int ty = ty0; ty <= ty1; ++ty)
+          for (int tz = tz0; tz <= tz1; ++tz)
+            atomicAdd(&A.tile_count[((int64_t)tx * A.ntile[1] + ty) * A.ntile[2] + tz], 1);
+    }
+  }
+  c_pm = warp_sum_d(c_pm);
+  c_mapped = (unsigned long long)warp_sum_ll((long long)c_mapped);
+  c_dep = (unsigned long long)warp_sum_ll((long long)c_dep);
+  flags = __reduce_or_sync(0xffffffffu, flags);
+  if (lane == 0) {
+    if (c_mapped) {
+      atomicAdd(&A.st->n_mapped, c_mapped);
+      atomicAdd(&A.st->deposits, c_dep);
+      atomicAdd(&A.st->particle_mass, c_pm);
+    }
+    if (flags) atomicOr(&A.st->flags, flags);
+  }
+}
+
+// K2: exclusive scan of the tile counts (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) k_scan_tiles(TiledArgs A) {
+  __shared__ long long part[1024];
+  const int64_t n = A.n_tiles;
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
+  long long s = 0;
+  for (int64_t i = b; i < e; ++i) s += A.tile_count[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+    long long v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int64_t i = b; i < e; ++i) {
+    A.tile_start[i] = run;
+    run += A.tile_count[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    A.tile_start[n] = part[blockDim.x - 1];
+    if (part[blockDim.x - 1] > A.pair_cap) atomicOr(&A.st->flags, kFlagOverflow);
+  }
+}
+
+// K3: one warp per record: renormalisation sum, weight factor, tile lists.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nrec = *A.n_rec;
+  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
+  const int nch = A.pt.nq + 1;
+  double c_gm = 0.0;
+  int emax[kMaxQ + 1];
+  for (int c = 0; c < nch; ++c) emax[c] = INT_MIN;
+  for (int64_t r = wid; r < nrec; r += nw) {
+    const int4 bx = A.box[r];
+    const int4 dm = A.dimv[r];
+    const float4 g = A.geo[r];
+    const int njk = dm.y * dm.z;
+    const int64_t F = (int64_t)dm.x * njk;
+    const float h = g.w, hinv = 1.0f / g.w;
+    // FP32 pass with a compensated per-lane sum
+    float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
+    for (int64_t f = lane; f < F; f += 32) {
+      const int a = (int)(f / njk);
+      const int rr = (int)(f - (int64_t)a * njk);
+      const int b = rr / dm.z, c = rr - b * dm.z;
+      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+      axis_f(g.x, h, a, &xd, &dx);
+      axis_f(g.y, h, b, &yd, &dy);
+      if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
+      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
+      const float u = sqrtf(d2) * hinv;
+      umin = fminf(umin, u);
+      if (u <= 1.0f) {
+        float t, e;
+        two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
+        s = t;
+        comp += e;
+      }
+    }
+    // compensated warp reduction
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, s, o);
+      const float co = __shfl_xor_sync(0xffffffffu, comp, o);
+      float t, e;
+      two_sum(s, so, t, e);
+      s = t;
+      comp = comp + co + e;
+      umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+    }
+    const double S = (double)s + (double)comp;
+    double cpv;
+    int fl = 0;
+    double bound;  // largest per-cell weight of this particle
+    double gm;
+    if (umin > 0.9f || !(S > 0.0)) {
+      // ill-conditioned (every pixel centre near or beyond the kernel edge):
+      // the reference's FP64 arithmetic, as in the plain path
+      PrepFP64 q;
+      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+      double s_w = 0.0, s_a = 0.0;
+      long long n_d = 0, n_t = 0;
+      for (int64_t f = lane; f < F; f += 32) {
+        const int a = (int)(f / njk);
+        const int rr = (int)(f - (int64_t)a * njk);
+        const int b = rr / dm.z, c = rr - b * dm.z;
+        double u, ar;
+        cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
+        s_a += ar;
+        n_t += 1;
+        if (u <= 1.0) {
+          s_w += kshape<KERN, double>(u) * q.knorm * ar;
+          n_d += 1;
+        }
+      }
+      s_w = warp_sum_d(s_w);
+      s_a = warp_sum_d(s_a);
+      n_d = warp_sum_ll(n_d);
+      n_t = warp_sum_ll(n_t);
+      const bool fallback = (s_w == 0.0);
+      double wpp;
+      if (fallback) {
+        n_d = n_t;
+        wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
+      } else {
+        wpp = (double)n_d / s_w;
+      }
+      cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                      : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
+      fl = kRecFP64 | (fallback ? kRecFallback : 0);
+      bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
+      gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    } else {
+      cpv = A.cp[r] / S;
+      bound = fabs(cpv);
+      gm = A.aux[r] * S;
+    }
+    if (lane == 0) {
+      A.cp[r] = cpv;
+      if (fl) A.box[r].w = fl;
+      c_gm += gm;
+      // scale exponents per channel
+      int e;
+      if (bound > 0.0 && bound < 1e300) {
+        frexp(bound, &e);
+        emax[A.pt.nq] = max(emax[A.pt.nq], e);
+        for (int k = 0; k < A.pt.nq; ++k) {
+          const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+          if (qa > 0.0 && qa < 1e300) {
+            frexp(bound * qa, &e);
+            emax[k] = max(emax[k], e);
+          }
+        }
+      }
+    }
+    // tile lists
+    if (!overflow) {
+      const int tx0 = bx.x / A.tdim[0], tx1 = (bx.x + dm.x - 1) / A.tdim[0];
+      const int ty0 = bx.y / A.tdim[1], ty1 = (bx.y + dm.y - 1) / A.tdim[1];
+      const int tz0 = bx.z / A.tdim[2], tz1 = (bx.z + dm.z - 1) / A.tdim[2];
+      const int nty = ty1 - ty0 + 1, ntz = tz1 - tz0 + 1;
+      const int nt = (tx1 - tx0 + 1) * nty * ntz;
+      for (int t = lane; t < nt; t += 32) {
+        const int ta = t / (nty * ntz), tb = (t / ntz) % nty, tc = t % ntz;
+        const int64_t tile = ((int64_t)(tx0 + ta) * A.ntile[1] + (ty0 + tb)) * A.ntile[2] + (tz0 + tc);
+        const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
+        A.pairs[slot] = (int)r;
+      }
+    }
+  }
+  if (lane == 0) {
+    if (DIMS == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
+    for (int c = 0; c < nch; ++c)
+      if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
+  }
+}
+
+// K4: one CTA per image tile.
+template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
+  constexpr int TV = TX * TY * TZ;
+  extern __shared__ float smem[];
+  const int nq = NQ > 0 ? NQ : A.pt.nq;
+  const int nch = nq + 1;
+  float* hi = smem;             // [nch][TV]
+  float* lo = smem + nch * TV;  // [nch][TV]
+  const int64_t t = blockIdx.x;
+  const int tz = (int)(t % A.ntile[2]);
+  const int ty = (int)((t / A.ntile[2]) % A.ntile[1]);
+  const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
+  const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
+  for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) smem[v] = 0.0f;
+  // channel scales (powers of two)
+  __shared__ double s_scale[kMaxQ + 1];
+  if (threadIdx.x < nch) {
+    const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
+    s_scale[threadIdx.x] = e < -100000 ? 1.0 : ldexp(1.0, kScaleTop - e);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const long long p0 = A.tile_start[t], p1 = A.tile_start[t + 1];
+  const double scw = s_scale[nq];
+  for (long long s = p0 + warp; s < p1; s += nwarp) {
+    const int r = A.pairs[s];
+    const int4 bx = A.box[r];
+    const int4 dm = A.dimv[r];
+    // intersection of the footprint with the tile, in footprint-local indices
+    const int a0 = max(0, ox - bx.x), a1 = min(dm.x, ox + TX - bx.x);
+    const int b0 = max(0, oy - bx.y), b1 = min(dm.y, oy + TY - bx.y);
+    const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
+    const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
+    const int n = na * nb * nc;
+    const double cpv = A.cp[r];
+    float cw = __double2float_rn(cpv * scw);
+    float cq[NQ > 0 ? NQ : kMaxQ];
+    for (int k = 0; k < nq; ++k)
+      cq[k] = __double2float_rn(cpv * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]);
+    const float inv_nc = 1.0f / (float)nc, inv_nb = 1.0f / (float)nb;
+    // local-frame offset of the tile origin
+    const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
+    if (bx.w & kRecFP64) {
+      // ill-conditioned particle: per-cell weights in the reference's FP64
+      PrepFP64 q;
+      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+      const bool fb = (bx.w & kRecFallback) != 0;
+      for (int e = lane; e < n; e += 32) {
+        const int bc = fdiv(e, inv_nc);
+        const int c = e - bc * nc;
+        const int a = fdiv(bc, inv_nb);
+        const int b = bc - a * nb;
+        const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
+        double u, ar;
+        cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
+        const double wk = fb ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * q.knorm : 0.0);
+        const double pw = wk * ar * cpv;
+        if (pw != 0.0) {
+          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+          acc_twosum(&hi[nq * TV + li], &lo[nq * TV + li], __double2float_rn(pw * scw));
+          for (int k = 0; k < nq; ++k)
+            acc_twosum(&hi[k * TV + li], &lo[k * TV + li],
+                       __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
+        }
+      }
+      continue;
+    }
+    const float4 g = A.geo[r];
+    const float h = g.w, hinv = 1.0f / g.w;
+    for (int e = lane; e < n; e += 32) {
+      const int bc = fdiv(e, inv_nc);
+      const int c = e - bc * nc;
+      const int a = fdiv(bc, inv_nb);
+      const int b = bc - a * nb;
+      const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
+      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+      axis_f(g.x, h, ia, &xd, &dx);
+      axis_f(g.y, h, jb, &yd, &dy);
+      if (DIMS == 3) axis_f(g.z, h, kc, &zd, &dz);
+      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
+      const float u = sqrtf(d2) * hinv;
+      if (u <= 1.0f) {
+        const float gw = kshape_f<KERN>(u) * (dx * dy * dz);
+        if (gw != 0.0f) {
+          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+          acc_twosum(&hi[nq * TV + li], &lo[nq * TV + li], gw * cw);
+#pragma unroll
+          for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+            if (NQ == 0 && k >= nq) break;
+            acc_twosum(&hi[k * TV + li], &lo[k * TV + li], gw * cq[k]);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // flush: FP64 values straight into the output layout
+  const int64_t P = A.mp.P;
+  const int64_t PD = DIMS == 2 ? P * P : P * P * P;
+  const double inv_w = 1.0 / scw;
+  for (int v = threadIdx.x; v < TV; v += blockDim.x) {
+    int li, i, j, k;
+    if (DIMS == 2 && A.mode == 0) {
+      // reduced 2D output is x-fastest: walk the tile x-fastest
+      const int ix = v % TX, iy = v / TX;
+      li = ix * TY + iy;
+      i = ox + ix;
+      j = oy + iy;
+      k = 0;
+    } else {
+      li = v;
+      i = ox + v / (TY * TZ);
+      j = oy + (v / TZ) % TY;
+      k = oz + v % TZ;
+    }
+    if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
+    const double W = ((double)hi[nq * TV + li] + (double)lo[nq * TV + li]) * inv_w;
+    if (DIMS == 3) {
+      double Q = ((double)hi[li] + (double)lo[li]) / s_scale[0];
+      if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
+      A.out[((int64_t)i * P + j) * P + k] = Q;
+    } else if (A.mode == 1) {
+      const int64_t row = (int64_t)i * P + j;
+      A.out[row + (int64_t)nq * PD] = W;
+      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = ((double)hi[c * TV + li] + (double)lo[c * TV + li]) / s_scale[c];
+    } else {
+      for (int c = 0; c < nq; ++c) {
+        double Q = ((double)hi[c * TV + li] + (double)lo[c * TV + li]) / s_scale[c];
+        if (A.reduce && W > 0.0) Q /= W;
+        A.out[(int64_t)i + P * j + PD * c] = Q;
+      }
+    }
+  }
+}
+
+template <int DIMS, int KERN, int NQ>
+void launch_deposit_nq(const TiledArgs& A, cudaStream_t s) {
+  if (DIMS == 2) {
+    constexpr int TX = 16, TY = 16;
+    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
+    k_deposit<2, KERN, NQ, TX, TY, 1><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+  } else {
+    constexpr int TX = 8, TY = 8, TZ = 8;
+    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
+    k_deposit<3, KERN, NQ, TX, TY, TZ><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+  }
+}
+
+template <int DIMS, int KERN>
+void launch_kern(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev) {
+  k_norm_fill<DIMS, KERN><<<grid_rec, 256, 0, s>>>(A);
+  if (ev) cudaEventRecord(ev[2], s);
+  switch (DIMS == 3 ? 1 : A.pt.nq) {
+    case 1: launch_deposit_nq<DIMS, KERN, 1>(A, s); break;
+    case 2: launch_deposit_nq<DIMS, KERN, 2>(A, s); break;
+    case 3: launch_deposit_nq<DIMS, KERN, 3>(A, s); break;
+    case 4: launch_deposit_nq<DIMS, KERN, 4>(A, s); break;
+    default: launch_deposit_nq<DIMS, KERN, 0>(A, s); break;
+  }
+}
+
+template <int DIMS>
+void launch_dims(int kernel, const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev) {
+  switch (kernel) {
+    case 0: launch_kern<DIMS, 0>(A, grid_rec, s, ev); break;
+    case 1: launch_kern<DIMS, 1>(A, grid_rec, s, ev); break;
+    case 2: launch_kern<DIMS, 2>(A, grid_rec, s, ev); break;
+    case 3: launch_kern<DIMS, 3>(A, grid_rec, s, ev); break;
+    default: launch_kern<DIMS, 4>(A, grid_rec, s, ev); break;
+  }
+}
+
+}  // namespace
+
+void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles) {
+  if (dims == 2) {
+    tdim[0] = 16; tdim[1] = 16; tdim[2] = 1;
+  } else {
+    tdim[0] = 8; tdim[1] = 8; tdim[2] = 8;
+  }
+  for (int d = 0; d < 3; ++d) ntile[d] = (d < dims) ? (int)((P + tdim[d] - 1) / tdim[d]) : 1;
+  *n_tiles = (int64_t)ntile[0] * ntile[1] * ntile[2];
+}
+
+// Launches K1..K4 on `s`.  With `ev` (4 events) the phases prep+scan,
+// norm+fill and deposit are bracketed for timing.  Returns the number of
+// kernels launched through `n_launch`.
+cudaError_t launch_tiled_fp32(int kernel, const TiledArgs& A, int num_sms, cudaStream_t s,
+                              cudaEvent_t* ev, int* n_launch) {
+  const int dims = A.mp.dims;
+  int grid = ceil_div(A.pt.n, 256);
+  if (grid > num_sms * 8) grid = num_sms * 8;
+  if (grid < 1) grid = 1;
+  if (ev) cudaEventRecord(ev[0], s);
+  if (dims == 2) k_prep_count<2><<<grid, 256, 0, s>>>(A);
+  else k_prep_count<3><<<grid, 256, 0, s>>>(A);
+  k_scan_tiles<<<1, 1024, 0, s>>>(A);
+  if (ev) cudaEventRecord(ev[1], s);
+  int grid_rec = ceil_div(A.pt.n, 8);
+  if (grid_rec > num_sms * 16) grid_rec = num_sms * 16;
+  if (grid_rec < 1) grid_rec = 1;
+  if (dims == 2) launch_dims<2>(kernel, A, grid_rec, s, ev);
+  else launch_dims<3>(kernel, A, grid_rec, s, ev);
+  if (ev) cudaEventRecord(ev[3], s);
+  if (n_launch) *n_launch = 4;
+  return cudaGetLastError();
+}
+
+}  // namespace sphg

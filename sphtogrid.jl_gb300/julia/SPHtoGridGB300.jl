@@ -1,0 +1,165 @@
+"""
+    SPHtoGridGB300
+
+Julia binding of libsphgrid.so (include/sphgrid.h): a drop-in `sphMapping`
+with the signature of SPHtoGrid.jl (src/cic_interpolation/cic_interpolation.jl:35-48)
+that maps on a GB300 GPU through `ccall`.
+
+    using SPHtoGrid, SPHKernels, SPHtoGridGB300
+    par = mappingParameters(x_lim=[0.0,1.0], y_lim=[0.0,1.0], z_lim=[0.0,1.0], Npixels=256)
+    img = SPHtoGridGB300.sphMapping(pos, hsml, m, rho, rho, rho; param=par, kernel=Cubic(2))
+
+The result has the reference's layout and type (`Array{Float64,3}`), `Pos` is
+centred in place as in the reference, and `precision = :fp32c` selects the
+FP32-compensated deposition.
+"""
+module SPHtoGridGB300
+
+using SPHtoGrid: mappingParameters
+using SPHKernels: AbstractSPHKernel, Cubic, Quintic, WendlandC4, WendlandC6, WendlandC8
+
+const libsphgrid = get(ENV, "SPHGRID_LIB", joinpath(@__DIR__, "..", "libsphgrid.so"))
+
+struct SphgParams
+    x_lim::NTuple{2,Float64}
+    y_lim::NTuple{2,Float64}
+    z_lim::NTuple{2,Float64}
+    center::NTuple{3,Float64}
+    halfsize::NTuple{3,Float64}
+    len2pix::Float64
+    pixelSideLength::Float64
+    Npixels::NTuple{3,Int64}
+    boxsize::Float64
+    periodic::Int32
+    pad_::Int32
+end
+
+SphgParams(p::mappingParameters) = SphgParams(
+    (Float64(p.x_lim[1]), Float64(p.x_lim[2])), (Float64(p.y_lim[1]), Float64(p.y_lim[2])),
+    (Float64(p.z_lim[1]), Float64(p.z_lim[2])),
+    (Float64(p.center[1]), Float64(p.center[2]), Float64(p.center[3])),
+    (Float64(p.halfsize[1]), Float64(p.halfsize[2]), Float64(p.halfsize[3])),
+    Float64(p.len2pix), Float64(p.pixelSideLength),
+    (Int64(p.Npixels[1]), Int64(p.Npixels[2]), Int64(p.Npixels[3])),
+    Float64(p.boxsize), Int32(p.periodic), Int32(0))
+
+struct SphgParticles
+    n::Int64
+    pos_dtype::Int32
+    attr_dtype::Int32
+    pos::Ptr{Cvoid}
+    pos_stride_p::Int64
+    pos_stride_c::Int64
+    hsml::Ptr{Cvoid}
+    mass::Ptr{Cvoid}
+    rho::Ptr{Cvoid}
+    weights::Ptr{Cvoid}
+    bin_q::Ptr{Cvoid}
+    n_q::Int32
+    pad_::Int32
+    q_stride_p::Int64
+    q_stride_k::Int64
+end
+
+struct SphgOptions
+    dimensions::Int32
+    kernel::Int32
+    kernel_dim::Int32
+    reduce_image::Int32
+    return_both_maps::Int32
+    calc_mean::Int32
+    precision::Int32
+    deterministic::Int32
+    center::Int32
+    filter::Int32
+    memspace::Int32
+    profile::Int32
+    reserved::NTuple{4,Int32}
+end
+
+mutable struct SphgStats
+    n_in::Int64
+    n_mapped::Int64
+    deposits::Int64
+    grid_mass::Float64
+    particle_mass::Float64
+    centred::SphgParams
+    n_launches::Int32
+    n_reruns::Int32
+    phase_ms::NTuple{4,Float32}
+    SphgStats() = new()
+end
+
+kernel_id(::Cubic) = 0
+kernel_id(::Quintic) = 1
+kernel_id(::WendlandC4) = 2
+kernel_id(::WendlandC6) = 3
+kernel_id(::WendlandC8) = 4
+
+dtype_id(::Type{Float32}) = Int32(0)
+dtype_id(::Type{Float64}) = Int32(1)
+
+const CTX = Ref{Ptr{Cvoid}}(C_NULL)
+
+function context()
+    if CTX[] == C_NULL
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        st = ccall((:sphg_context_create, libsphgrid), Cint, (Cint, Ref{Ptr{Cvoid}}), 0, h)
+        st == 0 || error(unsafe_string(ccall((:sphg_last_error, libsphgrid), Cstring, (Ptr{Cvoid},), C_NULL)))
+        CTX[] = h[]
+        atexit(() -> ccall((:sphg_context_destroy, libsphgrid), Cint, (Ptr{Cvoid},), CTX[]))
+    end
+    return CTX[]
+end
+
+"""
+    sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=Rho, RM=nothing;
+               param, kernel, show_progress=true, parallel=false, reduce_image=true,
+               return_both_maps=false, dimensions=2, calc_mean=false, stokes=false,
+               sort_z=false, precision=:fp64)
+
+The reference's `sphMapping` on the GPU.  `parallel` is ignored (one GPU);
+`RM`/`stokes` (Faraday rotation) and `sort_z` are not supported here.
+"""
+function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
+                    Rho::Array{<:Real}, Bin_Quant::Array{<:Real},
+                    Weights::Array{<:Real}=Rho, RM=nothing;
+                    param::mappingParameters, kernel::AbstractSPHKernel,
+                    show_progress::Bool=true, parallel::Bool=false,
+                    reduce_image::Bool=true, return_both_maps::Bool=false,
+                    dimensions::Int=2, calc_mean::Bool=false, stokes::Bool=false,
+                    sort_z::Bool=false, precision::Symbol=:fp64)
+    (RM === nothing && !stokes) || error("Faraday rotation is not supported by the GPU path")
+    sort_z && error("sort_z is not supported by the GPU path")
+    dimensions in (2, 3) || return nothing
+    T = (eltype(HSML) == Float32 && eltype(M) == Float32 && eltype(Rho) == Float32 &&
+         eltype(Bin_Quant) == Float32 && eltype(Weights) == Float32) ? Float32 : Float64
+    pos = eltype(Pos) <: Union{Float32,Float64} ? Pos : Float64.(Pos)
+    hsml, m, rho, w = T.(HSML), T.(M), T.(Rho), T.(Weights)
+    q = T.(Bin_Quant)
+    N = length(M)
+    nq = ndims(q) == 1 ? 1 : size(q, 1)
+    P = param.Npixels[1]
+    out = return_both_maps && dimensions == 2 ? zeros(Float64, P * P, nq + 1) :
+          dimensions == 2 ? zeros(Float64, P, P, nq) : zeros(Float64, P, P, P)
+    GC.@preserve pos hsml m rho w q out begin
+        pt = SphgParticles(N, dtype_id(eltype(pos)), dtype_id(T), pointer(pos), 3, 1,
+                           pointer(hsml), pointer(m), pointer(rho), pointer(w), pointer(q),
+                           Int32(nq), Int32(0), ndims(q) == 1 ? 1 : nq, ndims(q) == 1 ? 0 : 1)
+        kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
+        opt = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, return_both_maps,
+                          calc_mean, precision === :fp32c ? 1 : 0, 0, 1, 1, 1, 0, (0, 0, 0, 0))
+        st = SphgStats()
+        status = ccall((:sphg_map, libsphgrid), Cint,
+                       (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles},
+                        Ptr{Float64}, Ptr{Cvoid}, Ref{SphgStats}),
+                       context(), SphgParams(param), opt, pt, pointer(out), C_NULL, st)
+        status == 0 || error(unsafe_string(ccall((:sphg_last_error, libsphgrid), Cstring,
+                                                 (Ptr{Cvoid},), context())))
+    end
+    pos === Pos || (Pos .= pos)  # the reference centres the caller's array in place
+    show_progress && @info "Particles in image: $(st.n_mapped) / $N, deposits: $(st.deposits)"
+    return out
+end
+
+end # module

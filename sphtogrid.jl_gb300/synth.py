@@ -38,7 +38,30 @@ def uniform_2d(N=2 ** 18, npix=256, kernel="cubic", seed=0, dtype=np.float64):
     return d
 
 
-def clumps_3d(N=2 ** 22, npix=256, n_clumps=64, seed=0, dtype=np.float32, chunk=1 << 18):
+def _mixture_density(pos, cen, sig, counts, background):
+    """Number density of the clump mixture at each position (torch's
+    multithreaded elementwise ops on the host when available)."""
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    amp = counts / (2.0 * math.pi * sig ** 2) ** 1.5
+    if torch is not None:
+        p = torch.from_numpy(np.ascontiguousarray(pos.T))
+        out = torch.full((pos.shape[0],), background, dtype=torch.float64)
+        for c in range(cen.shape[0]):
+            r2 = (p[0] - cen[c, 0]) ** 2 + (p[1] - cen[c, 1]) ** 2 + (p[2] - cen[c, 2]) ** 2
+            out += amp[c] * torch.exp(r2 * (-0.5 / sig[c] ** 2))
+        return out.numpy()
+    pt = np.ascontiguousarray(pos.T)
+    out = np.full(pos.shape[0], background)
+    for c in range(cen.shape[0]):
+        r2 = (pt[0] - cen[c, 0]) ** 2 + (pt[1] - cen[c, 1]) ** 2 + (pt[2] - cen[c, 2]) ** 2
+        out += amp[c] * np.exp(r2 * (-0.5 / sig[c] ** 2))
+    return out
+
+
+def clumps_3d(N=2 ** 22, npix=256, n_clumps=64, seed=0, dtype=np.float32):
     """3D gridding workload: 64 isotropic Gaussian clumps (sigma 0.02-0.08)
     plus a 20% uniform background in the unit cube; hsml = 1.2 (32 / (4 pi/3
     n_local))^(1/3) from the analytic local number density, mass 1/N, rho
@@ -55,14 +78,7 @@ def clumps_3d(N=2 ** 22, npix=256, n_clumps=64, seed=0, dtype=np.float32, chunk=
     pos = np.concatenate([pc, rng.random((nb, 3))])
     perm = rng.permutation(N)
     pos = pos[perm]
-    # analytic number density of the mixture at each particle
-    nloc = np.empty(N)
-    norm = counts / (2.0 * math.pi * sig ** 2) ** 1.5
-    inv2s2 = 1.0 / (2.0 * sig ** 2)
-    for s in range(0, N, chunk):
-        p = pos[s:s + chunk]
-        r2 = ((p[:, None, :] - cen[None, :, :]) ** 2).sum(-1)
-        nloc[s:s + chunk] = nb + (norm[None, :] * np.exp(-r2 * inv2s2[None, :])).sum(1)
+    nloc = _mixture_density(pos, cen, sig, counts, float(nb))
     hsml = 1.2 * (32.0 / (4.0 * math.pi / 3.0 * nloc)) ** (1.0 / 3.0)
     rho = nloc / N  # mass 1/N times number density
     temp = np.exp(np.log(1e6) + rng.standard_normal(N))
