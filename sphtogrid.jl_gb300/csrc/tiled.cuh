@@ -55,6 +55,10 @@ struct TiledArgs {
   int* pairs;
   long long pair_cap;
   int* exps;        // per channel max exponent (channels 0..nq-1 = Q, nq = W)
+  // deterministic mode: exact int64 fixed-point tile sums
+  int det;
+  int* kexp;                  // K1: per channel max exponent of a particle's total
+  unsigned long long* bsum;   // K3: per channel integer bound of the channel total
   DevStatus* st;
   // output
   double* out;
@@ -95,6 +99,18 @@ __device__ __forceinline__ void acc_twosum(float* hi, float* lo, float v) {
   float s, e;
   two_sum(old, v, s, e);
   if (e != 0.0f) atomicAdd(lo, e);
+}
+
+// Fixed-point scale exponent of a channel in the deterministic mode: every
+// partial sum of the channel stays below 2^62 in magnitude.  The bound is the
+// integer sum (bsum + one unit per record) of per-particle totals in units of
+// 2^(kexp - 30), widened by 2^-20 for the FP32 rounding of the cell values.
+__device__ __forceinline__ int fixed_exponent(int kexp, unsigned long long bsum, int nrec) {
+  if (kexp < -100000 || bsum == 0ull) return 0;
+  const double bound = ldexp((double)bsum + (double)nrec + 1.0, kexp - 30) * (1.0 + 0x1p-20);
+  int e;
+  frexp(bound, &e);  // bound < 2^e
+  return 62 - e;
 }
 
 // FP32 kernel shape (no normalisation) via fused multiply-adds.

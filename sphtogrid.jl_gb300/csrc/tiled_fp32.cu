@@ -61,6 +61,21 @@ __global__ void __launch_bounds__(256) k_prep_count(TiledArgs A) {
       for (int k = 0; k < A.pt.nq; ++k)
         A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
             : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
+      if (A.det) {  // exponent of the particle's total per channel
+        const double num = fabs(A.cp[r]);
+        int e;
+        if (num > 0.0 && num < 1e300) {
+          frexp(num, &e);
+          atomicMax(&A.kexp[A.pt.nq], e);
+          for (int k = 0; k < A.pt.nq; ++k) {
+            const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+            if (qa > 0.0 && qa < 1e300) {
+              frexp(num * qa, &e);
+              atomicMax(&A.kexp[k], e);
+            }
+          }
+        }
+      }
       // (particle, tile) overlaps
       const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
       const int ty0 = j0 / A.tdim[1], ty1 = (j0 + nj - 1) / A.tdim[1];
@@ -163,6 +178,16 @@ __global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
       umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
     }
     const double S = (double)s + (double)comp;
+    if (A.det && lane == 0) {  // deterministic channel bounds (integer sums)
+      const double num = fabs(A.cp[r]);
+      if (num > 0.0 && num < 1e300) {
+        for (int c = 0; c < nch; ++c) {
+          const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
+          if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
+            atomicAdd(&A.bsum[c], (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c])));
+        }
+      }
+    }
     double cpv;
     int fl = 0;
     double bound;  // largest per-cell weight of this particle
@@ -249,26 +274,49 @@ __global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
   }
 }
 
-// K4: one CTA per image tile.
-template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ>
+// Adds one cell value to a tile accumulator (see k_deposit).
+template <bool DET>
+__device__ __forceinline__ void acc_cell(float* hi, float* lo, unsigned long long* fx, int i, float v) {
+  if (DET) {
+    atomicAdd(&fx[i], (unsigned long long)__float2ll_rn(v));
+  } else {
+    acc_twosum(&hi[i], &lo[i], v);
+  }
+}
+
+template <bool DET>
+__device__ __forceinline__ double cell_value(const float* hi, const float* lo, const unsigned long long* fx, int i) {
+  if (DET) return (double)(long long)fx[i];
+  return (double)hi[i] + (double)lo[i];
+}
+
+// K4: one CTA per image tile.  DET selects exact int64 fixed-point tile sums
+// (bitwise reproducible) instead of TwoSum-compensated FP32 (hi, lo) pairs;
+// both use 8 bytes per channel and tile pixel.
+template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
   constexpr int TV = TX * TY * TZ;
-  extern __shared__ float smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nq = NQ > 0 ? NQ : A.pt.nq;
   const int nch = nq + 1;
-  float* hi = smem;             // [nch][TV]
-  float* lo = smem + nch * TV;  // [nch][TV]
+  float* hi = (float*)smem_raw;             // [nch][TV]
+  float* lo = hi + nch * TV;                // [nch][TV]
+  unsigned long long* fx = (unsigned long long*)smem_raw;  // DET: [nch][TV]
   const int64_t t = blockIdx.x;
   const int tz = (int)(t % A.ntile[2]);
   const int ty = (int)((t / A.ntile[2]) % A.ntile[1]);
   const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
   const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
-  for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) smem[v] = 0.0f;
+  for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
   // channel scales (powers of two)
   __shared__ double s_scale[kMaxQ + 1];
   if (threadIdx.x < nch) {
-    const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
-    s_scale[threadIdx.x] = e < -100000 ? 1.0 : ldexp(1.0, kScaleTop - e);
+    if (DET) {
+      s_scale[threadIdx.x] = ldexp(1.0, fixed_exponent(A.kexp[threadIdx.x], A.bsum[threadIdx.x], *A.n_rec));
+    } else {
+      const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
+      s_scale[threadIdx.x] = e < -100000 ? 1.0 : ldexp(1.0, kScaleTop - e);
+    }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -309,10 +357,10 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
         const double pw = wk * ar * cpv;
         if (pw != 0.0) {
           const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
-          acc_twosum(&hi[nq * TV + li], &lo[nq * TV + li], __double2float_rn(pw * scw));
+          acc_cell<DET>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
           for (int k = 0; k < nq; ++k)
-            acc_twosum(&hi[k * TV + li], &lo[k * TV + li],
-                       __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
+            acc_cell<DET>(hi, lo, fx, k * TV + li,
+                          __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
         }
       }
       continue;
@@ -335,11 +383,11 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
         const float gw = kshape_f<KERN>(u) * (dx * dy * dz);
         if (gw != 0.0f) {
           const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
-          acc_twosum(&hi[nq * TV + li], &lo[nq * TV + li], gw * cw);
+          acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
           for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
             if (NQ == 0 && k >= nq) break;
-            acc_twosum(&hi[k * TV + li], &lo[k * TV + li], gw * cq[k]);
+            acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
           }
         }
       }
@@ -366,18 +414,18 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
       k = oz + v % TZ;
     }
     if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
-    const double W = ((double)hi[nq * TV + li] + (double)lo[nq * TV + li]) * inv_w;
+    const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
     if (DIMS == 3) {
-      double Q = ((double)hi[li] + (double)lo[li]) / s_scale[0];
+      double Q = cell_value<DET>(hi, lo, fx, li) / s_scale[0];
       if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
       A.out[((int64_t)i * P + j) * P + k] = Q;
     } else if (A.mode == 1) {
       const int64_t row = (int64_t)i * P + j;
       A.out[row + (int64_t)nq * PD] = W;
-      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = ((double)hi[c * TV + li] + (double)lo[c * TV + li]) / s_scale[c];
+      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
     } else {
       for (int c = 0; c < nq; ++c) {
-        double Q = ((double)hi[c * TV + li] + (double)lo[c * TV + li]) / s_scale[c];
+        double Q = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
         if (A.reduce && W > 0.0) Q /= W;
         A.out[(int64_t)i + P * j + PD * c] = Q;
       }
@@ -385,17 +433,23 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
   }
 }
 
-template <int DIMS, int KERN, int NQ>
-void launch_deposit_nq(const TiledArgs& A, cudaStream_t s) {
+template <int DIMS, int KERN, int NQ, bool DET>
+void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
   if (DIMS == 2) {
     constexpr int TX = 16, TY = 16;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
-    k_deposit<2, KERN, NQ, TX, TY, 1><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+    k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   } else {
     constexpr int TX = 8, TY = 8, TZ = 8;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
-    k_deposit<3, KERN, NQ, TX, TY, TZ><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+    k_deposit<3, KERN, NQ, TX, TY, TZ, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   }
+}
+
+template <int DIMS, int KERN, int NQ>
+void launch_deposit_nq(const TiledArgs& A, cudaStream_t s) {
+  if (A.det) launch_deposit_det<DIMS, KERN, NQ, true>(A, s);
+  else launch_deposit_det<DIMS, KERN, NQ, false>(A, s);
 }
 
 template <int DIMS, int KERN>

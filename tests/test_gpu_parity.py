@@ -369,3 +369,33 @@ def test_fp32c_clumps_3d_full_size(gpu):
     assert sa["deposits"] == sb["deposits"] and sa["n_mapped"] == sb["n_mapped"]
     assert rel_linf(a, b, FLOOR) <= TOL["fp32c"]
     assert math.isclose(sa["grid_mass"], sb["grid_mass"], rel_tol=1e-5)
+
+
+# ------------------------------------------------------- deterministic mode
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_deterministic_mode_is_bitwise_reproducible(gpu, oracle, dims):
+    case = _case(41, 3000 if dims == 2 else 900, nq=2 if dims == 2 else 1, qneg=True)
+    P = 40 if dims == 2 else 20
+    kw = dict(precision="fp32c", deterministic=True)
+    if dims == 2:
+        kw["return_both_maps"] = True
+    a, _, sa, _ = _compare(gpu, oracle, case, P, dims, "wendlandc4", **kw)
+    b, _, sb, _ = _compare(gpu, oracle, case, P, dims, "wendlandc4", **kw)
+    assert np.array_equal(a, b)  # same bits, whatever the atomic order
+
+
+def test_deterministic_full_size_2d(gpu, oracle):
+    from sphtogrid_gb300 import synth
+    d = synth.uniform_2d()
+    par = gpu.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=256)
+    outs = []
+    for _ in range(2):
+        outs.append(gpu.sphMapping(d["pos"].copy(order="F"), d["hsml"], d["mass"], d["rho"],
+                                   d["bin_q"], d["weights"], param=par, kernel=gpu.Cubic(2),
+                                   show_progress=False, precision="fp32c", deterministic=True))
+    assert np.array_equal(outs[0], outs[1])
+    opar = oracle.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=256)
+    ref, _ = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["mass"], d["rho"],
+                                d["bin_q"], d["weights"], param=opar, kernel="cubic", kernel_dim=2)
+    assert rel_linf(outs[0], ref, FLOOR) <= TOL["fp32c"]
