@@ -23,6 +23,12 @@ void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one
 
 // Tile shape and tile counts of the FP32-compensated path.
 void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles);
+// K3 + K4 for one kernel shape (tiled_k<K>.cu).
+void launch_norm_deposit_0(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
+void launch_norm_deposit_1(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
+void launch_norm_deposit_2(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
+void launch_norm_deposit_3(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
+void launch_norm_deposit_4(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
 cudaError_t launch_tiled_fp32(int kernel, const TiledArgs& A, int num_sms, cudaStream_t s,
                               cudaEvent_t* ev, int* n_launch);
 

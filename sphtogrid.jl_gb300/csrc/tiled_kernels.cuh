@@ -1,0 +1,364 @@
+// tiled_kernels.cuh -- templates of the per-kernel-shape passes of the
+// FP32-compensated tiled deposition: K3 k_norm_fill and K4 k_deposit (see
+// tiled.cuh).  Each tiled_k<K>.cu instantiates them for one SPHKernels shape
+// so the build compiles the shapes in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <climits>
+
+#include "internal.h"
+#include "tiled.cuh"
+
+namespace sphg {
+namespace tiled_detail {
+
+// K3: one warp per record: renormalisation sum, weight factor, tile lists.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nrec = *A.n_rec;
+  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
+  const int nch = A.pt.nq + 1;
+  double c_gm = 0.0;
+  int emax[kMaxQ + 1];
+  for (int c = 0; c < nch; ++c) emax[c] = INT_MIN;
+  for (int64_t r = wid; r < nrec; r += nw) {
+    const int4 bx = A.box[r];
+    const int4 dm = A.dimv[r];
+    const float4 g = A.geo[r];
+    const int njk = dm.y * dm.z;
+    const int64_t F = (int64_t)dm.x * njk;
+    const float h = g.w, hinv = 1.0f / g.w;
+    // FP32 pass with a compensated per-lane sum
+    float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
+    for (int64_t f = lane; f < F; f += 32) {
+      const int a = (int)(f / njk);
+      const int rr = (int)(f - (int64_t)a * njk);
+      const int b = rr / dm.z, c = rr - b * dm.z;
+      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+      axis_f(g.x, h, a, &xd, &dx);
+      axis_f(g.y, h, b, &yd, &dy);
+      if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
+      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
+      const float u = sqrtf(d2) * hinv;
+      umin = fminf(umin, u);
+      if (u <= 1.0f) {
+        float t, e;
+        two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
+        s = t;
+        comp += e;
+      }
+    }
+    // compensated warp reduction
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float so = __shfl_xor_sync(0xffffffffu, s, o);
+      const float co = __shfl_xor_sync(0xffffffffu, comp, o);
+      float t, e;
+      two_sum(s, so, t, e);
+      s = t;
+      comp = comp + co + e;
+      umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+    }
+    const double S = (double)s + (double)comp;
+    if (A.det && lane == 0) {  // deterministic channel bounds (integer sums)
+      const double num = fabs(A.cp[r]);
+      if (num > 0.0 && num < 1e300) {
+        for (int c = 0; c < nch; ++c) {
+          const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
+          if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
+            atomicAdd(&A.bsum[c], (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c])));
+        }
+      }
+    }
+    double cpv;
+    int fl = 0;
+    double bound;  // largest per-cell weight of this particle
+    double gm;
+    if (umin > 0.9f || !(S > 0.0)) {
+      // ill-conditioned (every pixel centre near or beyond the kernel edge):
+      // the reference's FP64 arithmetic, as in the plain path
+      PrepFP64 q;
+      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+      double s_w = 0.0, s_a = 0.0;
+      long long n_d = 0, n_t = 0;
+      for (int64_t f = lane; f < F; f += 32) {
+        const int a = (int)(f / njk);
+        const int rr = (int)(f - (int64_t)a * njk);
+        const int b = rr / dm.z, c = rr - b * dm.z;
+        double u, ar;
+        cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
+        s_a += ar;
+        n_t += 1;
+        if (u <= 1.0) {
+          s_w += kshape<KERN, double>(u) * q.knorm * ar;
+          n_d += 1;
+        }
+      }
+      s_w = warp_sum_d(s_w);
+      s_a = warp_sum_d(s_a);
+      n_d = warp_sum_ll(n_d);
+      n_t = warp_sum_ll(n_t);
+      const bool fallback = (s_w == 0.0);
+      double wpp;
+      if (fallback) {
+        n_d = n_t;
+        wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
+      } else {
+        wpp = (double)n_d / s_w;
+      }
+      cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                      : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
+      fl = kRecFP64 | (fallback ? kRecFallback : 0);
+      bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
+      gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    } else {
+      cpv = A.cp[r] / S;
+      bound = fabs(cpv);
+      gm = A.aux[r] * S;
+    }
+    if (lane == 0) {
+      A.cp[r] = cpv;
+      if (fl) A.box[r].w = fl;
+      c_gm += gm;
+      // scale exponents per channel
+      int e;
+      if (bound > 0.0 && bound < 1e300) {
+        frexp(bound, &e);
+        emax[A.pt.nq] = max(emax[A.pt.nq], e);
+        for (int k = 0; k < A.pt.nq; ++k) {
+          const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+          if (qa > 0.0 && qa < 1e300) {
+            frexp(bound * qa, &e);
+            emax[k] = max(emax[k], e);
+          }
+        }
+      }
+    }
+    // tile lists
+    if (!overflow) {
+      const int tx0 = bx.x / A.tdim[0], tx1 = (bx.x + dm.x - 1) / A.tdim[0];
+      const int ty0 = bx.y / A.tdim[1], ty1 = (bx.y + dm.y - 1) / A.tdim[1];
+      const int tz0 = bx.z / A.tdim[2], tz1 = (bx.z + dm.z - 1) / A.tdim[2];
+      const int nty = ty1 - ty0 + 1, ntz = tz1 - tz0 + 1;
+      const int nt = (tx1 - tx0 + 1) * nty * ntz;
+      for (int t = lane; t < nt; t += 32) {
+        const int ta = t / (nty * ntz), tb = (t / ntz) % nty, tc = t % ntz;
+        const int64_t tile = ((int64_t)(tx0 + ta) * A.ntile[1] + (ty0 + tb)) * A.ntile[2] + (tz0 + tc);
+        const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
+        A.pairs[slot] = (int)r;
+      }
+    }
+  }
+  if (lane == 0) {
+    if (DIMS == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
+    for (int c = 0; c < nch; ++c)
+      if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
+  }
+}
+
+// Adds one cell value to a tile accumulator (see k_deposit).
+template <bool DET>
+__device__ __forceinline__ void acc_cell(float* hi, float* lo, unsigned long long* fx, int i, float v) {
+  if (DET) {
+    atomicAdd(&fx[i], (unsigned long long)__float2ll_rn(v));
+  } else {
+    acc_twosum(&hi[i], &lo[i], v);
+  }
+}
+
+template <bool DET>
+__device__ __forceinline__ double cell_value(const float* hi, const float* lo, const unsigned long long* fx, int i) {
+  if (DET) return (double)(long long)fx[i];
+  return (double)hi[i] + (double)lo[i];
+}
+
+// K4: one CTA per image tile.  DET selects exact int64 fixed-point tile sums
+// (bitwise reproducible) instead of TwoSum-compensated FP32 (hi, lo) pairs;
+// both use 8 bytes per channel and tile pixel.
+template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
+__global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
+  constexpr int TV = TX * TY * TZ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nq = NQ > 0 ? NQ : A.pt.nq;
+  const int nch = nq + 1;
+  float* hi = (float*)smem_raw;             // [nch][TV]
+  float* lo = hi + nch * TV;                // [nch][TV]
+  unsigned long long* fx = (unsigned long long*)smem_raw;  // DET: [nch][TV]
+  const int64_t t = blockIdx.x;
+  const int tz = (int)(t % A.ntile[2]);
+  const int ty = (int)((t / A.ntile[2]) % A.ntile[1]);
+  const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
+  const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
+  for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
+  // channel scales (powers of two)
+  __shared__ double s_scale[kMaxQ + 1];
+  if (threadIdx.x < nch) {
+    if (DET) {
+      s_scale[threadIdx.x] = ldexp(1.0, fixed_exponent(A.kexp[threadIdx.x], A.bsum[threadIdx.x], *A.n_rec));
+    } else {
+      const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
+      s_scale[threadIdx.x] = e < -100000 ? 1.0 : ldexp(1.0, kScaleTop - e);
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const long long p0 = A.tile_start[t], p1 = A.tile_start[t + 1];
+  const double scw = s_scale[nq];
+  for (long long s = p0 + warp; s < p1; s += nwarp) {
+    const int r = A.pairs[s];
+    const int4 bx = A.box[r];
+    const int4 dm = A.dimv[r];
+    // intersection of the footprint with the tile, in footprint-local indices
+    const int a0 = max(0, ox - bx.x), a1 = min(dm.x, ox + TX - bx.x);
+    const int b0 = max(0, oy - bx.y), b1 = min(dm.y, oy + TY - bx.y);
+    const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
+    const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
+    const int n = na * nb * nc;
+    const double cpv = A.cp[r];
+    float cw = __double2float_rn(cpv * scw);
+    float cq[NQ > 0 ? NQ : kMaxQ];
+    for (int k = 0; k < nq; ++k)
+      cq[k] = __double2float_rn(cpv * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]);
+    const float inv_nc = 1.0f / (float)nc, inv_nb = 1.0f / (float)nb;
+    // local-frame offset of the tile origin
+    const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
+    if (bx.w & kRecFP64) {
+      // ill-conditioned particle: per-cell weights in the reference's FP64
+      PrepFP64 q;
+      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+      const bool fb = (bx.w & kRecFallback) != 0;
+      for (int e = lane; e < n; e += 32) {
+        const int bc = fdiv(e, inv_nc);
+        const int c = e - bc * nc;
+        const int a = fdiv(bc, inv_nb);
+        const int b = bc - a * nb;
+        const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
+        double u, ar;
+        cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
+        const double wk = fb ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * q.knorm : 0.0);
+        const double pw = wk * ar * cpv;
+        if (pw != 0.0) {
+          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+          acc_cell<DET>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
+          for (int k = 0; k < nq; ++k)
+            acc_cell<DET>(hi, lo, fx, k * TV + li,
+                          __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
+        }
+      }
+      continue;
+    }
+    const float4 g = A.geo[r];
+    const float h = g.w, hinv = 1.0f / g.w;
+    for (int e = lane; e < n; e += 32) {
+      const int bc = fdiv(e, inv_nc);
+      const int c = e - bc * nc;
+      const int a = fdiv(bc, inv_nb);
+      const int b = bc - a * nb;
+      const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
+      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+      axis_f(g.x, h, ia, &xd, &dx);
+      axis_f(g.y, h, jb, &yd, &dy);
+      if (DIMS == 3) axis_f(g.z, h, kc, &zd, &dz);
+      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
+      const float u = sqrtf(d2) * hinv;
+      if (u <= 1.0f) {
+        const float gw = kshape_f<KERN>(u) * (dx * dy * dz);
+        if (gw != 0.0f) {
+          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+          acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+#pragma unroll
+          for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+            if (NQ == 0 && k >= nq) break;
+            acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // flush: FP64 values straight into the output layout
+  const int64_t P = A.mp.P;
+  const int64_t PD = DIMS == 2 ? P * P : P * P * P;
+  const double inv_w = 1.0 / scw;
+  for (int v = threadIdx.x; v < TV; v += blockDim.x) {
+    int li, i, j, k;
+    if (DIMS == 2 && A.mode == 0) {
+      // reduced 2D output is x-fastest: walk the tile x-fastest
+      const int ix = v % TX, iy = v / TX;
+      li = ix * TY + iy;
+      i = ox + ix;
+      j = oy + iy;
+      k = 0;
+    } else {
+      li = v;
+      i = ox + v / (TY * TZ);
+      j = oy + (v / TZ) % TY;
+      k = oz + v % TZ;
+    }
+    if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
+    const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
+    if (DIMS == 3) {
+      double Q = cell_value<DET>(hi, lo, fx, li) / s_scale[0];
+      if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
+      A.out[((int64_t)i * P + j) * P + k] = Q;
+    } else if (A.mode == 1) {
+      const int64_t row = (int64_t)i * P + j;
+      A.out[row + (int64_t)nq * PD] = W;
+      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
+    } else {
+      for (int c = 0; c < nq; ++c) {
+        double Q = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
+        if (A.reduce && W > 0.0) Q /= W;
+        A.out[(int64_t)i + P * j + PD * c] = Q;
+      }
+    }
+  }
+}
+
+template <int DIMS, int KERN, int NQ, bool DET>
+void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
+  if (DIMS == 2) {
+    constexpr int TX = 16, TY = 16;
+    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
+    k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+  } else {
+    constexpr int TX = 8, TY = 8, TZ = 8;
+    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
+    k_deposit<3, KERN, NQ, TX, TY, TZ, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
+  }
+}
+
+template <int DIMS, int KERN, int NQ>
+void launch_deposit_nq(const TiledArgs& A, cudaStream_t s) {
+  if (A.det) launch_deposit_det<DIMS, KERN, NQ, true>(A, s);
+  else launch_deposit_det<DIMS, KERN, NQ, false>(A, s);
+}
+
+template <int DIMS, int KERN>
+inline void launch_kern(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev) {
+  k_norm_fill<DIMS, KERN><<<grid_rec, 256, 0, s>>>(A);
+  if (ev) cudaEventRecord(ev[2], s);
+  switch (DIMS == 3 ? 1 : A.pt.nq) {
+    case 1: launch_deposit_nq<DIMS, KERN, 1>(A, s); break;
+    case 2: launch_deposit_nq<DIMS, KERN, 2>(A, s); break;
+    case 3: launch_deposit_nq<DIMS, KERN, 3>(A, s); break;
+    case 4: launch_deposit_nq<DIMS, KERN, 4>(A, s); break;
+    default: launch_deposit_nq<DIMS, KERN, 0>(A, s); break;
+  }
+}
+
+}  // namespace tiled_detail
+
+// Instantiates launch_norm_deposit_<K> (declared in internal.h).
+#define SPHG_TILED_SHAPE(K)                                                                     \
+  void launch_norm_deposit_##K(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev) { \
+    if (A.mp.dims == 2) tiled_detail::launch_kern<2, K>(A, grid_rec, s, ev);                   \
+    else tiled_detail::launch_kern<3, K>(A, grid_rec, s, ev);                                  \
+  }
+
+}  // namespace sphg
