@@ -124,7 +124,10 @@ typedef struct sphg_options {
                                reference's filter); 0: map every particle */
   int32_t memspace;         /* SPHG_MEM_*: where pos/attrs/out live */
   int32_t profile;          /* 1: time the phases with CUDA events (sphg_stats.phase_ms) */
-  int32_t reserved[4];      /* must be 0 */
+  int32_t raw_accumulator;  /* 1: write the raw (P^D, Nq+1) accumulator [Q_1..Q_Nq, W] in
+                               2D and 3D (2D: same as return_both_maps); the reference's
+                               3D path has no such output */
+  int32_t reserved[3];      /* must be 0 */
 } sphg_options;
 
 /* Phases timed with sphg_options.profile (device time on the call's stream). */
@@ -176,11 +179,36 @@ int sphg_mapping_parameters(const double x_lim[2], const double y_lim[2],
 /* Number of doubles sphg_map writes to `out` for these options. */
 int64_t sphg_output_len(const sphg_params *par, const sphg_options *opt, int32_t n_q);
 
+/* Gradients of a map with respect to the particle inputs (FP64, device
+ * memory).  pos and bin_q use the strides of the sphg_particles they belong to. */
+typedef struct sphg_grads {
+  double *pos;
+  double *hsml, *mass, *rho, *weights;
+  double *bin_q;
+} sphg_grads;
+
 /* sphMapping (cic_interpolation.jl:35-272): centre, filter, deposit, reduce.
  * `stream` is a cudaStream_t (NULL: the context's own stream).  The call
  * returns after the result is complete in `out`.  `stats` may be NULL. */
 int sphg_map(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
              const sphg_particles *parts, double *out, void *stream, sphg_stats *stats);
+
+/* reduce_image_2D / reduce_image_3D (reduce_image.jl:8-55) of a raw
+ * (P^D, Nq+1) accumulator into the output layout of `opt` (device memory). */
+int sphg_reduce(sphg_context *ctx, const sphg_params *par, const sphg_options *opt, int32_t n_q,
+                const double *raw, double *out, void *stream);
+
+/* Adjoint of sphg_map (no counterpart in the reference, which has no
+ * derivatives): given the forward's raw accumulator `raw` ((P^D, Nq+1), from
+ * raw_accumulator = 1) and dL/d(output) `grad_out` in the layout of the
+ * output `opt` describes, writes dL/d(pos, hsml, mass, rho, weights, bin_q)
+ * into `grads`.  Kernel weights are recomputed, not stored.  Particles the
+ * forward skips (filtered out, or q == 0 without calc_mean) get zero
+ * gradients.  Device memory only; positions must be centred the way the
+ * forward saw them (use SPHG_CENTER_READONLY in both, or NONE after INPLACE). */
+int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
+                 const sphg_particles *parts, const double *raw, const double *grad_out,
+                 const sphg_grads *grads, void *stream);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,10 @@ def lib():
                                       vp, vp, vp, vp, i32, i64, i64, vp, i64, i32, i32, i32, i32, i32,
                                       vp, dp, C.POINTER(C.c_int64)]
         L.orc_sph_mapping.restype = i32
+        L.orc_particle_contrib.argtypes = [i32, C.POINTER(OrcParams), i32, i32, C.c_double, C.c_double,
+                                           C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                           i64, vp, vp]
+        L.orc_particle_contrib.restype = i64
         _lib = L
     return _lib
 
@@ -193,9 +197,20 @@ def footprints(dims, par, pos, hsml, q, calc_mean=False):
     return rng, state
 
 
+def particle_contrib(dims, par, kernel, kdim, x, y, z, hsml, m, rho, w, cap=1 << 22):
+    """(flat pixel indices, weights pw) of one particle with centred position."""
+    idx = np.zeros(cap, dtype=np.int64)
+    pw = np.zeros(cap)
+    n = lib().orc_particle_contrib(dims, C.byref(par), KERNELS[kernel], kdim, x, y, z, hsml, m,
+                                   rho, w, cap, idx.ctypes.data, pw.ctypes.data)
+    if n < 0:
+        raise OracleError("particle_contrib failed")
+    return idx[:n].copy(), pw[:n].copy()
+
+
 def sph_mapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param: OrcParams, kernel="cubic",
                 kernel_dim=None, reduce_image=True, return_both_maps=False, dimensions=2,
-                calc_mean=False, sort_z=False, nthreads=1, copy_pos=True):
+                calc_mean=False, sort_z=False, nthreads=1, copy_pos=True, raw3d=False):
     """Oracle ``sphMapping`` (cic_interpolation.jl:35-272).
 
     Positions are centred in place as in the reference unless ``copy_pos``.
@@ -216,7 +231,7 @@ def sph_mapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param: OrcParams,
     if dimensions == 2:
         out = np.zeros(P * P * (nq + 1) if return_both_maps else P * P * nq)
     elif dimensions == 3:
-        out = np.zeros(P ** 3)
+        out = np.zeros(2 * P ** 3 if raw3d else P ** 3)
     else:
         raise OracleError(ERRORS[3])
     par = OrcParams.from_buffer_copy(param)
@@ -226,13 +241,16 @@ def sph_mapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param: OrcParams,
     st = lib().orc_sph_mapping(C.byref(par), dimensions, KERNELS[kernel], kdim, _dtype_code(pos),
                                pos.ctypes.data, sp, sc, _dtype_code(hsml), hsml.ctypes.data,
                                m.ctypes.data, rho.ctypes.data, q.ctypes.data, nq, qsp, qsc,
-                               w.ctypes.data, pos.shape[1], int(reduce_image), int(return_both_maps),
+                               w.ctypes.data, pos.shape[1], int(reduce_image),
+                               2 if (raw3d and dimensions == 3) else int(return_both_maps),
                                int(calc_mean), int(sort_z), int(nthreads), out.ctypes.data,
                                C.byref(gm), C.byref(dep))
     if st:
         raise OracleError(ERRORS[st])
     if dimensions == 2 and return_both_maps:
         image = out.reshape((P * P, nq + 1), order="F")
+    elif dimensions == 3 and raw3d:
+        image = out.reshape((P ** 3, 2), order="F")
     elif dimensions == 2:
         image = out.reshape((P, P, nq), order="F")
     else:

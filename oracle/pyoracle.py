@@ -8,7 +8,9 @@ bit for bit.
 Follows src/cic_interpolation/cic_2D.jl:11-244, cic_3D.jl:13-208,
 cic_shared.jl:9-121, reduce_image.jl:8-55 and shared/indices.jl of
 SPHtoGrid.jl.  Inputs are already centred and filtered; the particle order is
-the order of the arrays.
+the order of the arrays.  Inputs may be any number type with the arithmetic
+operators (the adjoint tests pass dual numbers: forward-mode derivatives of
+this restatement).
 """
 from __future__ import annotations
 
@@ -60,8 +62,22 @@ def W(kernel: str, kdim: int, u: float, h_inv: float) -> float:
     return (t8 * t2 * (1.0 + 10.0 * u + 42.0 * u2 + 90.0 * (u2 * u) + 429.0 / 5.0 * (u2 * u2))) * n
 
 
+def _num(v):
+    """Plain floats for numpy scalars; other number types (the dual numbers of
+    the adjoint tests) pass through."""
+    return v if hasattr(v, "d") else float(v)
+
+
+def _val(v):
+    return v.v if hasattr(v, "d") else v
+
+
+def _sqrt(v):
+    return v.sqrt() if hasattr(v, "sqrt") else math.sqrt(v)
+
+
 def _range(x, h, P):
-    return max(math.floor(x - h), 0), min(math.floor(x + h), P - 1)
+    return max(math.floor(_val(x - h)), 0), min(math.floor(_val(x + h)), P - 1)
 
 
 def _overlap(x, h, i):
@@ -77,22 +93,22 @@ def cic_map(dims, pos, hsml, m, rho, q, w, L, P, kernel, kdim=None, calc_mean=Fa
     chans = [dict() for _ in range(nq + 1)]
     deposits = 0
     for p in range(len(m)):
-        bq = [float(v) for v in q[p]]
+        bq = [_num(v) for v in q[p]]
         allzero = all(v == 0.0 for v in bq)
         if allzero and not calc_mean:
             continue
-        h = float(hsml[p]) * L
+        h = _num(hsml[p]) * L
         h_inv = 1.0 / h
         if dims == 2:
             area = (2.0 * h) * (2.0 * h)
-            rho_pix = float(rho[p]) * (1.0 / (L * L * L))
-            col = float(m[p]) / rho_pix / area
+            rho_pix = _num(rho[p]) * (1.0 / (L * L * L))
+            col = _num(m[p]) / rho_pix / area
         else:
-            rho_pix = float(rho[p]) / (L * L * L)
-            vol = float(m[p]) / rho_pix
+            rho_pix = _num(rho[p]) / (L * L * L)
+            vol = _num(m[p]) / rho_pix
         c = []
         for d in range(3):
-            v = float(pos[p][d]) * L
+            v = _num(pos[p][d]) * L
             v += 0.5 * float(P)
             c.append(v)
         rngs = [_range(c[d], h, P) for d in range(dims)]
@@ -113,10 +129,10 @@ def cic_map(dims, pos, hsml, m, rho, q, w, L, P, kernel, kdim=None, calc_mean=Fa
             dist = [c[d] - float(cell[d]) - 0.5 for d in range(dims)]
             ov = [_overlap(c[d], h, cell[d]) for d in range(dims)]
             if dims == 2:
-                u = math.sqrt(dist[0] * dist[0] + dist[1] * dist[1]) * h_inv
+                u = _sqrt(dist[0] * dist[0] + dist[1] * dist[1]) * h_inv
                 a = ov[0] * ov[1]
             else:
-                u = math.sqrt(dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2]) * h_inv
+                u = _sqrt(dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2]) * h_inv
                 a = ov[0] * ov[1] * ov[2]
             A.append(a)
             s_a += a
@@ -135,9 +151,9 @@ def cic_map(dims, pos, hsml, m, rho, q, w, L, P, kernel, kdim=None, calc_mean=Fa
         else:
             wpp = n_d / s_w
         if dims == 2:
-            norm = area / n_d * wpp * float(w[p]) * col
+            norm = area / n_d * wpp * _num(w[p]) * col
         else:
-            norm = vol / n_d * wpp * float(w[p]) * L
+            norm = vol / n_d * wpp * _num(w[p]) * L
         for t, cell in enumerate(cells):
             idx = cell[0] * P + cell[1] if dims == 2 else cell[0] * P * P + cell[1] * P + cell[2]
             pw = wk[t] * A[t] * norm

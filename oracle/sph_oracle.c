@@ -635,6 +635,10 @@ int orc_sph_mapping(orc_params *par_io, int dims, int kernel, int kdim,
         memcpy(out, img, (size_t)img_len * sizeof(double));
       else
         orc_reduce_image_2d(img, P0, nq, reduce_image, out);
+    } else if (return_both_maps == 2) {
+      /* raw (P^3, 2) accumulator: not an output of the reference (its 3D path
+       * always reduces); used to check adjoints */
+      memcpy(out, img, (size_t)img_len * sizeof(double));
     } else {
       if (!reduce_image)
         for (int64_t e = 0; e < PD; ++e) img[PD + e] = 1.0; /* :230-232 */
@@ -648,4 +652,47 @@ int orc_sph_mapping(orc_params *par_io, int dims, int kernel, int kdim,
   free(img);
   free(order);
   return status;
+}
+
+/* ------------------------------------------------- one particle's weights */
+
+/* Weights pw of ONE particle (attributes given as doubles, position already
+ * centred) on its footprint pixels: idx[t] (flat, x slowest) and pw[t] for
+ * t < return value (-1 on error / capacity).  The same arithmetic as
+ * cic_run, used to take finite differences of a loss particle by particle. */
+int64_t orc_particle_contrib(int dims, const orc_params *par, int kernel, int kdim, double px,
+                             double py, double pz, double hsml_in, double m_in, double rho_in,
+                             double w_in, int64_t cap, int64_t *idx, double *pw) {
+  const int64_t P = par->Npixels[0];
+  const int64_t PD = dims == 2 ? P * P : P * P * P;
+  double pos[3] = {px, py, pz};
+  double one = 1.0;
+  int64_t order = 0;
+  double *img = (double *)calloc((size_t)PD * 2, sizeof(double));
+  if (!img) return -1;
+  cic_job J;
+  memset(&J, 0, sizeof(J));
+  J.dims = dims; J.kernel = kernel; J.kdim = kdim; J.calc_mean = 0; J.nq = 1;
+  J.par = par; J.pos_dtype = ORC_F64; J.attr_dtype = ORC_F64;
+  J.pos = pos; J.sp = 3; J.sc = 1;
+  J.hsml = &hsml_in; J.m = &m_in; J.rho = &rho_in; J.w = &w_in; J.q = &one;
+  J.q_sp = 1; J.q_sc = 0; J.order = &order; J.n_order = 1; J.image = img;
+  cic_run(&J);
+  free(J.wk);
+  free(J.A);
+  int64_t n = 0;
+  if (J.status == ORC_OK) {
+    for (int64_t e = 0; e < PD; ++e) {
+      if (img[PD + e] != 0.0) {
+        if (n >= cap) { n = -1; break; }
+        idx[n] = e;
+        pw[n] = img[PD + e];
+        ++n;
+      }
+    }
+  } else {
+    n = -1;
+  }
+  free(img);
+  return n;
 }

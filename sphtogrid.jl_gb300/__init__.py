@@ -11,6 +11,14 @@ from .parameters import (Cubic, MappingParameters, Quintic, SPHKernel, WendlandC
                          WendlandC6, WendlandC8, kernel_from_name, mappingParameters)
 from .mapping import sphMapping  # noqa: F401
 
+
+def __getattr__(name):
+    # torch is only needed for the differentiable path
+    if name in ("sph_map_differentiable", "SPHMapFunction"):
+        from . import autograd
+        return getattr(autograd, name)
+    raise AttributeError(name)
+
 __all__ = ["mappingParameters", "MappingParameters", "sphMapping", "Cubic", "Quintic",
            "WendlandC4", "WendlandC6", "WendlandC8", "SPHKernel", "kernel_from_name",
            "SPHtoGridError", "Context", "default_context"]

@@ -84,7 +84,8 @@ class SphgOptions(C.Structure):
         ("filter", C.c_int32),
         ("memspace", C.c_int32),
         ("profile", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("raw_accumulator", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -99,6 +100,17 @@ class SphgStats(C.Structure):
         ("n_launches", C.c_int32),
         ("n_reruns", C.c_int32),
         ("phase_ms", C.c_float * 4),
+    ]
+
+
+class SphgGrads(C.Structure):
+    _fields_ = [
+        ("pos", C.c_void_p),
+        ("hsml", C.c_void_p),
+        ("mass", C.c_void_p),
+        ("rho", C.c_void_p),
+        ("weights", C.c_void_p),
+        ("bin_q", C.c_void_p),
     ]
 
 
@@ -146,6 +158,11 @@ def lib():
         L.sphg_map.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
                                C.POINTER(SphgParticles), vp, vp, C.POINTER(SphgStats)]
         L.sphg_map.restype = i32
+        L.sphg_reduce.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions), i32, vp, vp, vp]
+        L.sphg_reduce.restype = i32
+        L.sphg_adjoint.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
+                                   C.POINTER(SphgParticles), vp, vp, C.POINTER(SphgGrads), vp]
+        L.sphg_adjoint.restype = i32
         _lib = L
     return _lib
 

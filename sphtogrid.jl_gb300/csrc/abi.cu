@@ -244,8 +244,9 @@ int sphg_mapping_parameters(const double x_lim_in[2], const double y_lim_in[2], 
 int64_t sphg_output_len(const sphg_params* par, const sphg_options* opt, int32_t n_q) {
   if (!par || !opt) return -1;
   const int64_t P = par->Npixels[0];
-  if (opt->dimensions == 2) return opt->return_both_maps ? P * P * (n_q + 1) : P * P * n_q;
-  if (opt->dimensions == 3) return P * P * P;
+  const bool raw = opt->raw_accumulator || (opt->dimensions == 2 && opt->return_both_maps);
+  if (opt->dimensions == 2) return raw ? P * P * (n_q + 1) : P * P * n_q;
+  if (opt->dimensions == 3) return raw ? 2 * P * P * P : P * P * P;
   return -1;
 }
 
@@ -266,7 +267,7 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   if (opt->center < 0 || opt->center > 2) return fail(ctx, SPHG_ERR_ARG, "unknown center mode");
   if (opt->memspace != SPHG_MEM_DEVICE && opt->memspace != SPHG_MEM_HOST)
     return fail(ctx, SPHG_ERR_ARG, "unknown memspace");
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < 3; ++r)
     if (opt->reserved[r]) return fail(ctx, SPHG_ERR_ARG, "reserved option fields must be 0");
   if (!valid_dtype(pt->pos_dtype) || !valid_dtype(pt->attr_dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
   const int64_t n = pt->n;
@@ -300,6 +301,7 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   const bool host = opt->memspace == SPHG_MEM_HOST;
   const bool fp32c = opt->precision == SPHG_PREC_FP32C;
+  const bool raw_out = opt->raw_accumulator || (dims == 2 && opt->return_both_maps);
   const size_t psz = dtype_size(pt->pos_dtype), asz = dtype_size(pt->attr_dtype);
   const int64_t pos_span = n > 0 ? (n - 1) * pt->pos_stride_p + 2 * pt->pos_stride_c + 1 : 0;
   const int64_t q_span = n > 0 ? (n - 1) * pt->q_stride_p + (int64_t)(nq - 1) * pt->q_stride_k + 1 : 0;
@@ -326,9 +328,9 @@ again:
   }
   // FP64 path accumulator: 2D raw maps accumulate straight into the output,
   // 3D keeps Q in the output and only the weight channel in the workspace.
-  const bool acc_in_out = (dims == 2 && opt->return_both_maps) || dims == 3;
+  const bool acc_in_out = raw_out || dims == 3;
   size_t o_acc = 0;
-  if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 ? PD : 0) : PD * (nq + 1)) * sizeof(double));
+  if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 && !raw_out ? PD : 0) : PD * (nq + 1)) * sizeof(double));
   size_t o_box = 0, o_dim = 0, o_geo = 0, o_cp = 0, o_aux = 0, o_qv = 0, o_cnt = 0, o_start = 0,
          o_pairs = 0, o_nrec = 0, o_exps = 0;
   const int64_t cap = n > 0 ? n : 1;
@@ -408,7 +410,7 @@ again:
   if (!fp32c) {
     double* acc;  // (nq+1) channels of PD doubles
     double* acc_w;
-    if (dims == 2 && opt->return_both_maps) {
+    if (raw_out) {
       acc = dout;
       acc_w = dout + (int64_t)nq * PD;
     } else if (dims == 3) {
@@ -418,7 +420,7 @@ again:
       acc = (double*)(ws + o_acc);
       acc_w = acc + (int64_t)nq * PD;
     }
-    if (dims == 3) {
+    if (dims == 3 && !raw_out) {
       CK(cudaMemsetAsync(acc, 0, PD * sizeof(double), s));
       CK(cudaMemsetAsync(acc_w, 0, PD * sizeof(double), s));
     } else {
@@ -432,14 +434,13 @@ again:
     sphg::launch_plain_fp64(opt->kernel, d, mp, acc, acc_w, PD, ctx->d_status, ctx->num_sms, s);
     CK(cudaGetLastError());
     if (ev) CK(cudaEventRecord(ev[3], s));
-    if (dims == 2) {
-      if (!opt->return_both_maps) sphg::launch_reduce_2d(acc, P, nq, opt->reduce_image, dout, s);
-    } else {
-      sphg::launch_reduce_3d(acc, acc_w, PD, opt->reduce_image ? 0 : 1, dout, ctx->num_sms, s);
+    if (!raw_out) {
+      if (dims == 2) sphg::launch_reduce_2d(acc, P, nq, opt->reduce_image, dout, s);
+      else sphg::launch_reduce_3d(acc, acc_w, PD, opt->reduce_image ? 0 : 1, dout, ctx->num_sms, s);
     }
     CK(cudaGetLastError());
     if (ev) CK(cudaEventRecord(ev[4], s));
-    n_launch = (dims == 2 && opt->return_both_maps) ? 1 : 2;
+    n_launch = raw_out ? 1 : 2;
   } else {
     ta.pt = d;
     ta.mp = mp;
@@ -464,7 +465,7 @@ again:
     ta.det = opt->deterministic ? 1 : 0;
     ta.st = ctx->d_status;
     ta.out = dout;
-    ta.mode = dims == 3 ? 2 : (opt->return_both_maps ? 1 : 0);
+    ta.mode = raw_out ? 1 : (dims == 3 ? 2 : 0);
     ta.reduce = opt->reduce_image;
     ta.w_is_one = opt->reduce_image ? 0 : 1;
     CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 1) * sizeof(int), s));
@@ -506,6 +507,107 @@ again:
   }
   if (hs.flags & sphg::kFlagNonFinite) return fail(ctx, SPHG_ERR_NONFINITE, "");
   if (hs.flags & sphg::kFlagTimeout) return fail(ctx, SPHG_ERR_TIMEOUT, "");
+  ctx->last_error.clear();
+  return SPHG_OK;
+}
+
+int sphg_reduce(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, int32_t n_q,
+                const double* raw, double* out, void* stream) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!par || !opt || !raw || !out) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
+  const int dims = opt->dimensions;
+  if (dims != 2 && dims != 3) return fail(ctx, SPHG_ERR_DIMS, "");
+  if (n_q < 1 || n_q > sphg::kMaxQ || (dims == 3 && n_q != 1)) return fail(ctx, SPHG_ERR_NQ, "");
+  const int64_t P = par->Npixels[0];
+  const int64_t PD = dims == 2 ? P * P : P * P * P;
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  if (dims == 2) sphg::launch_reduce_2d(raw, P, n_q, opt->reduce_image, out, s);
+  else sphg::launch_reduce_3d(raw, raw + PD, PD, opt->reduce_image ? 0 : 1, out, ctx->num_sms, s);
+  CK(cudaGetLastError());
+  if (!stream) CK(cudaStreamSynchronize(s));
+  return SPHG_OK;
+}
+
+int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
+                 const sphg_particles* pt, const double* raw, const double* grad_out,
+                 const sphg_grads* gr, void* stream) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!par || !opt || !pt || !raw || !grad_out || !gr) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
+  if (opt->memspace != SPHG_MEM_DEVICE) return fail(ctx, SPHG_ERR_UNSUPPORTED, "adjoint takes device memory");
+  const int dims = opt->dimensions;
+  if (dims != 2 && dims != 3) return fail(ctx, SPHG_ERR_DIMS, "");
+  const int nq = pt->n_q;
+  if (nq < 1 || nq > sphg::kMaxQ) return fail(ctx, SPHG_ERR_ARG, "n_q must be in 1..16");
+  if (dims == 3 && nq != 1) return fail(ctx, SPHG_ERR_NQ, "");
+  if (opt->kernel < 0 || opt->kernel > 4 || (opt->kernel_dim != 2 && opt->kernel_dim != 3))
+    return fail(ctx, SPHG_ERR_ARG, "kernel");
+  if (!valid_dtype(pt->pos_dtype) || !valid_dtype(pt->attr_dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
+  const int64_t n = pt->n;
+  if (n < 0) return fail(ctx, SPHG_ERR_ARG, "negative particle count");
+  if (n > 0 && (!pt->pos || !pt->hsml || !pt->mass || !pt->rho || !pt->weights || !pt->bin_q || !gr->pos ||
+                !gr->hsml || !gr->mass || !gr->rho || !gr->weights || !gr->bin_q))
+    return fail(ctx, SPHG_ERR_ARG, "NULL particle or gradient array");
+  const int64_t P = par->Npixels[0];
+  if (P < 1 || P > (int64_t)1 << 20 || (dims == 3 && P > 4096)) return fail(ctx, SPHG_ERR_ARG, "Npixels");
+  const int64_t PD = dims == 2 ? P * P : P * P * P;
+  sphg_params cpar;
+  {
+    const double* cen = par->center;
+    const double xl[2] = {par->x_lim[0] - cen[0], par->x_lim[1] - cen[0]};
+    const double yl[2] = {par->y_lim[0] - cen[1], par->y_lim[1] - cen[1]};
+    const double zl[2] = {par->z_lim[0] - cen[2], par->z_lim[1] - cen[2]};
+    const double c0[3] = {0.0, 0.0, 0.0};
+    int64_t Pmax = par->Npixels[0];
+    if (par->Npixels[1] > Pmax) Pmax = par->Npixels[1];
+    if (par->Npixels[2] > Pmax) Pmax = par->Npixels[2];
+    int st = sphg_mapping_parameters(xl, yl, zl, c0, -1.0, -1.0, -1.0, -1.0, Pmax, par->boxsize, &cpar);
+    if (st) return fail(ctx, st, g_error);
+  }
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  Carve cv;
+  const size_t o_g = cv.take((size_t)PD * (nq + 1) * sizeof(double));
+  if (int st = ensure_ws(ctx, cv.off, s)) return st;
+  double* gq = (double*)((char*)ctx->ws + o_g);
+  double* gw = gq + (int64_t)nq * PD;
+  sphg::DevParticles d;
+  d.n = n;
+  d.pos_dtype = pt->pos_dtype;
+  d.attr_dtype = pt->attr_dtype;
+  d.pos = pt->pos;
+  d.sp = pt->pos_stride_p;
+  d.sc = pt->pos_stride_c;
+  d.hsml = pt->hsml;
+  d.mass = pt->mass;
+  d.rho = pt->rho;
+  d.w = pt->weights;
+  d.q = pt->bin_q;
+  d.nq = nq;
+  d.qsp = pt->q_stride_p;
+  d.qsk = pt->q_stride_k;
+  sphg::DevMapParams mp;
+  for (int k = 0; k < 3; ++k) {
+    mp.cen[k] = par->center[k];
+    mp.lo[k] = cpar.center[k] - cpar.halfsize[k];
+    mp.hi[k] = cpar.center[k] + cpar.halfsize[k];
+  }
+  mp.boxsize = par->boxsize;
+  mp.periodic = par->periodic;
+  mp.center_mode = opt->center == SPHG_CENTER_INPLACE ? SPHG_CENTER_READONLY : opt->center;
+  mp.filter = opt->filter;
+  mp.calc_mean = dims == 2 ? opt->calc_mean : 0;
+  mp.kernel_dim = opt->kernel_dim;
+  mp.dims = dims;
+  mp.L = cpar.len2pix;
+  mp.P = P;
+  mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
+  const bool raw_out = opt->raw_accumulator || (dims == 2 && opt->return_both_maps);
+  CK(sphg::launch_adjoint(opt->kernel, d, mp, raw, grad_out, raw_out ? 1 : 0, opt->reduce_image, gq, gw,
+                          gr->pos, gr->hsml, gr->mass, gr->rho, gr->weights, gr->bin_q, ctx->num_sms, s));
+  if (!stream) CK(cudaStreamSynchronize(s));
   ctx->last_error.clear();
   return SPHG_OK;
 }

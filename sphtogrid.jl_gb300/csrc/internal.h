@@ -23,6 +23,11 @@ void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one
 
 // Tile shape and tile counts of the FP32-compensated path.
 void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles);
+cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParams& mp, const double* raw,
+                           const double* grad_out, int mode, int reduce, double* gq, double* gw,
+                           double* d_pos, double* d_hsml, double* d_mass, double* d_rho, double* d_w,
+                           double* d_q, int num_sms, cudaStream_t s);
+
 // K3 + K4 for one kernel shape (tiled_k<K>.cu).
 void launch_norm_deposit_0(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
 void launch_norm_deposit_1(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);

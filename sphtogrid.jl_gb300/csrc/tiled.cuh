@@ -62,7 +62,7 @@ struct TiledArgs {
   DevStatus* st;
   // output
   double* out;
-  int mode;         // 0: 2D reduced, 1: 2D raw accumulator, 2: 3D reduced
+  int mode;         // 0: 2D reduced, 1: raw (P^D, nq+1) accumulator, 2: 3D reduced
   int reduce;       // 2D reduce_image
   int w_is_one;     // 3D !reduce_image
 };

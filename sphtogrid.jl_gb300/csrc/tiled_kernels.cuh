@@ -302,14 +302,14 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
     }
     if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
     const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
-    if (DIMS == 3) {
+    if (A.mode == 1) {  // raw (P^D, nq+1) accumulator
+      const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
+      A.out[row + (int64_t)nq * PD] = W;
+      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
+    } else if (DIMS == 3) {
       double Q = cell_value<DET>(hi, lo, fx, li) / s_scale[0];
       if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
       A.out[((int64_t)i * P + j) * P + k] = Q;
-    } else if (A.mode == 1) {
-      const int64_t row = (int64_t)i * P + j;
-      A.out[row + (int64_t)nq * PD] = W;
-      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
     } else {
       for (int c = 0; c < nq; ++c) {
         double Q = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
