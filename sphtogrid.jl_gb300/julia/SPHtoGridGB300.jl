@@ -162,4 +162,72 @@ function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
     return out
 end
 
+# ---------------------------------------------------------------- adjoint
+
+struct SphgGrads
+    pos::Ptr{Cvoid}
+    hsml::Ptr{Cvoid}
+    mass::Ptr{Cvoid}
+    rho::Ptr{Cvoid}
+    weights::Ptr{Cvoid}
+    bin_q::Ptr{Cvoid}
+end
+
+using ChainRulesCore: ChainRulesCore, NoTangent, unthunk
+
+"""
+    rrule(::typeof(sphMapping_differentiable), Pos, HSML, M, Rho, Bin_Quant, Weights; kw...)
+
+ChainRulesCore rule of the GPU map (device arrays, `CuArray`s).  The forward
+deposits into the raw accumulator (`raw_accumulator = 1`), reduces it with
+`sphg_reduce`, and keeps the accumulator; the pullback calls `sphg_adjoint`,
+which recomputes the kernel weights instead of storing the particle-pixel
+list and returns dL/d(Pos, HSML, M, Rho, Bin_Quant, Weights).
+"""
+function sphMapping_differentiable end
+
+function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M, Rho, Bin_Quant,
+                              Weights; param::mappingParameters, kernel::AbstractSPHKernel,
+                              dimensions::Int=2, reduce_image::Bool=true, precision::Symbol=:fp64)
+    CUDA = Base.require(Base.PkgId(Base.UUID("052768ef-5323-5732-b1bb-66c8b64840ba"), "CUDA"))
+    T = eltype(HSML)
+    N = length(M)
+    nq = ndims(Bin_Quant) == 1 ? 1 : size(Bin_Quant, 1)
+    P = param.Npixels[1]
+    PD = dimensions == 2 ? P^2 : P^3
+    raw = CUDA.zeros(Float64, PD * (nq + 1))
+    out = dimensions == 2 ? CUDA.zeros(Float64, P, P, nq) : CUDA.zeros(Float64, P, P, P)
+    kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
+    mkopt(raw_acc) = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, false, false,
+                                 precision === :fp32c ? 1 : 0, 0, 2, 1, 0, 0, (raw_acc, 0, 0, 0))
+    ptr(a) = reinterpret(Ptr{Cvoid}, pointer(a))
+    pt = SphgParticles(N, dtype_id(eltype(Pos)), dtype_id(T), ptr(Pos), 3, 1, ptr(HSML), ptr(M),
+                       ptr(Rho), ptr(Weights), ptr(Bin_Quant), Int32(nq), Int32(0),
+                       ndims(Bin_Quant) == 1 ? 1 : nq, ndims(Bin_Quant) == 1 ? 0 : 1)
+    st = SphgStats()
+    s = ccall((:sphg_map, libsphgrid), Cint,
+              (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles}, Ptr{Cvoid},
+               Ptr{Cvoid}, Ref{SphgStats}),
+              context(), SphgParams(param), mkopt(1), pt, ptr(raw), C_NULL, st)
+    s == 0 || error("sphg_map failed with status $s")
+    s = ccall((:sphg_reduce, libsphgrid), Cint,
+              (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+              context(), SphgParams(param), mkopt(0), Int32(nq), ptr(raw), ptr(out), C_NULL)
+    s == 0 || error("sphg_reduce failed with status $s")
+    function pullback(dout)
+        g = CUDA.CuArray{Float64}(unthunk(dout))
+        dpos = CUDA.zeros(Float64, size(Pos))
+        dh, dm, dr, dw = (CUDA.zeros(Float64, N) for _ in 1:4)
+        dq = CUDA.zeros(Float64, size(Bin_Quant))
+        gr = SphgGrads(ptr(dpos), ptr(dh), ptr(dm), ptr(dr), ptr(dw), ptr(dq))
+        s = ccall((:sphg_adjoint, libsphgrid), Cint,
+                  (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles}, Ptr{Cvoid},
+                   Ptr{Cvoid}, Ref{SphgGrads}, Ptr{Cvoid}),
+                  context(), SphgParams(param), mkopt(0), pt, ptr(raw), ptr(g), gr, C_NULL)
+        s == 0 || error("sphg_adjoint failed with status $s")
+        return (NoTangent(), dpos, dh, dm, dr, dq, dw)
+    end
+    return out, pullback
+end
+
 end # module
