@@ -368,7 +368,7 @@ again:
     d.w = ws + o_w;
     d.q = ws + o_q;
     dout = (double*)(ws + o_out);
-    if (n > 0 && rerun == 0) {
+    if (n > 0) {  // every pass: a re-run may have reallocated the workspace
       CK(cudaMemcpyAsync(ws + o_pos, pt->pos, pos_span * psz, cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(ws + o_h, pt->hsml, n * asz, cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(ws + o_m, pt->mass, n * asz, cudaMemcpyHostToDevice, s));
@@ -394,8 +394,9 @@ again:
   mp.boxsize = par->boxsize;
   mp.periodic = par->periodic;
   mp.center_mode = opt->center;
-  // a re-run after K1 already wrote centred positions back must not centre again
-  if (rerun && opt->center == SPHG_CENTER_INPLACE) mp.center_mode = SPHG_CENTER_NONE;
+  // a re-run after K1 already centred the caller's device positions in place
+  // must not centre again (host inputs are copied afresh on every pass)
+  if (rerun && !host && opt->center == SPHG_CENTER_INPLACE) mp.center_mode = SPHG_CENTER_NONE;
   mp.filter = opt->filter;
   mp.calc_mean = dims == 2 ? opt->calc_mean : 0;  // cic_mapping_3D gets no calc_mean (:219)
   mp.kernel_dim = opt->kernel_dim;

@@ -207,7 +207,10 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const long long p0 = A.tile_start[t], p1 = A.tile_start[t + 1];
+  // after an overflow of the pair list the lists are incomplete: deposit
+  // nothing (the host grows the list and maps again)
+  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
+  const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
   const double scw = s_scale[nq];
   for (long long s = p0 + warp; s < p1; s += nwarp) {
     const int r = A.pairs[s];

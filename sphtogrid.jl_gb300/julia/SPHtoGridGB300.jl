@@ -74,7 +74,8 @@ struct SphgOptions
     filter::Int32
     memspace::Int32
     profile::Int32
-    reserved::NTuple{4,Int32}
+    raw_accumulator::Int32
+    reserved::NTuple{3,Int32}
 end
 
 mutable struct SphgStats
@@ -148,7 +149,7 @@ function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
                            Int32(nq), Int32(0), ndims(q) == 1 ? 1 : nq, ndims(q) == 1 ? 0 : 1)
         kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
         opt = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, return_both_maps,
-                          calc_mean, precision === :fp32c ? 1 : 0, 0, 1, 1, 1, 0, (0, 0, 0, 0))
+                          calc_mean, precision === :fp32c ? 1 : 0, 0, 1, 1, 1, 0, 0, (0, 0, 0))
         st = SphgStats()
         status = ccall((:sphg_map, libsphgrid), Cint,
                        (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles},
@@ -199,7 +200,7 @@ function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M,
     out = dimensions == 2 ? CUDA.zeros(Float64, P, P, nq) : CUDA.zeros(Float64, P, P, P)
     kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
     mkopt(raw_acc) = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, false, false,
-                                 precision === :fp32c ? 1 : 0, 0, 2, 1, 0, 0, (raw_acc, 0, 0, 0))
+                                 precision === :fp32c ? 1 : 0, 0, 2, 1, 0, 0, raw_acc, (0, 0, 0))
     ptr(a) = reinterpret(Ptr{Cvoid}, pointer(a))
     pt = SphgParticles(N, dtype_id(eltype(Pos)), dtype_id(T), ptr(Pos), 3, 1, ptr(HSML), ptr(M),
                        ptr(Rho), ptr(Weights), ptr(Bin_Quant), Int32(nq), Int32(0),

@@ -79,7 +79,9 @@ def _shape_out(flat, P, nq, dims, raw):
 def _stats_dict(st: _lib.SphgStats):
     return {"n_in": st.n_in, "n_mapped": st.n_mapped, "deposits": st.deposits,
             "grid_mass": st.grid_mass, "particle_mass": st.particle_mass,
-            "centred_param": MappingParameters(_lib.SphgParams.from_buffer_copy(st.centred))}
+            "centred_param": MappingParameters(_lib.SphgParams.from_buffer_copy(st.centred)),
+            "n_launches": st.n_launches, "n_reruns": st.n_reruns,
+            "phase_ms": list(st.phase_ms)}
 
 def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: MappingParameters,
                kernel: SPHKernel, show_progress: bool = True, parallel: bool = False,
