@@ -123,7 +123,8 @@ class SPHtoGridError(RuntimeError):
 
 
 _lib = None
-_lock = threading.Lock()
+# re-entrant: default_context() holds it while Context() loads the library
+_lock = threading.RLock()
 
 
 def lib():

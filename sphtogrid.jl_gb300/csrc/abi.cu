@@ -24,6 +24,7 @@ struct sphg_context {
   sphg::DevStatus* d_status = nullptr;
   sphg::DevStatus* h_status = nullptr;  // pinned
   size_t pair_cap = 0;                  // FP32C tile-pair list capacity (grow-only)
+  size_t chunk_cap = 0;                 // FP32C large-record chunk capacity (grow-only)
   cudaEvent_t ev[5] = {};               // phase timing events
 };
 
@@ -312,6 +313,8 @@ int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   int rerun = 0;
   long long pair_cap = (long long)ctx->pair_cap;
   if (fp32c && pair_cap < 8 * n + ta.n_tiles) pair_cap = 8 * n + ta.n_tiles;
+  long long chunk_cap = (long long)ctx->chunk_cap;
+  if (fp32c && chunk_cap < 4096) chunk_cap = 4096;
 
 again:
   // workspace layout
@@ -332,7 +335,7 @@ again:
   size_t o_acc = 0;
   if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 && !raw_out ? PD : 0) : PD * (nq + 1)) * sizeof(double));
   size_t o_box = 0, o_dim = 0, o_geo = 0, o_cp = 0, o_aux = 0, o_qv = 0, o_cnt = 0, o_start = 0,
-         o_pairs = 0, o_nrec = 0, o_exps = 0;
+         o_pairs = 0, o_nrec = 0, o_exps = 0, o_large = 0, o_lstart = 0, o_part = 0;
   const int64_t cap = n > 0 ? n : 1;
   if (fp32c) {
     o_box = cv.take(cap * sizeof(int4));
@@ -341,11 +344,14 @@ again:
     o_cp = cv.take(cap * sizeof(double));
     o_aux = cv.take(cap * sizeof(double));
     o_qv = cv.take(cap * nq * sizeof(float));
-    o_cnt = cv.take((2 * ta.n_tiles + 1) * sizeof(int));  // counts, fill, record counter
+    o_cnt = cv.take((2 * ta.n_tiles + 2) * sizeof(int));  // counts, fill, record and large counters
     o_start = cv.take((ta.n_tiles + 1) * sizeof(long long));
     o_pairs = cv.take(pair_cap * sizeof(int));
     o_nrec = o_cnt + 2 * ta.n_tiles * sizeof(int);
     o_exps = cv.take(2 * (sphg::kMaxQ + 1) * sizeof(int) + (sphg::kMaxQ + 1) * sizeof(unsigned long long));
+    o_large = cv.take(cap * sizeof(int));
+    o_lstart = cv.take((cap + 1) * sizeof(long long));
+    o_part = cv.take(chunk_cap * sizeof(float4));
   }
   if (int st = ensure_ws(ctx, cv.off, s)) return st;
   char* ws = (char*)ctx->ws;
@@ -464,12 +470,18 @@ again:
     ta.kexp = ta.exps + (sphg::kMaxQ + 1);
     ta.bsum = (unsigned long long*)(ta.kexp + (sphg::kMaxQ + 1));
     ta.det = opt->deterministic ? 1 : 0;
+    ta.n_large = ta.n_rec + 1;
+    ta.large = (int*)(ws + o_large);
+    ta.large_start = (long long*)(ws + o_lstart);
+    ta.partials = (float4*)(ws + o_part);
+    ta.chunk_cap = chunk_cap;
+    ta.large_grid = ctx->num_sms * 4;
     ta.st = ctx->d_status;
     ta.out = dout;
     ta.mode = raw_out ? 1 : (dims == 3 ? 2 : 0);
     ta.reduce = opt->reduce_image;
     ta.w_is_one = opt->reduce_image ? 0 : 1;
-    CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 1) * sizeof(int), s));
+    CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 2) * sizeof(int), s));
     CK(cudaMemsetAsync(ta.exps, 0x80, 2 * (sphg::kMaxQ + 1) * sizeof(int), s));
     CK(cudaMemsetAsync(ta.bsum, 0, (sphg::kMaxQ + 1) * sizeof(unsigned long long), s));
     CK(sphg::launch_tiled_fp32(opt->kernel, ta, ctx->num_sms, s, ev, &n_launch));
@@ -484,15 +496,22 @@ again:
   CK(cudaStreamSynchronize(s));
   const sphg::DevStatus hs = *ctx->h_status;
   if (fp32c && (hs.flags & sphg::kFlagOverflow) && !(hs.flags & sphg::kFlagNonFinite)) {
-    // more (particle, tile) pairs than the list holds: grow it and map again
-    long long total = 0;
+    // more (particle, tile) pairs or large-record chunks than the lists hold:
+    // grow them and map again
+    long long total = 0, chunks = 0;
+    int nl = 0;
     CK(cudaMemcpy(&total, ta.tile_start + ta.n_tiles, sizeof(long long), cudaMemcpyDeviceToHost));
-    pair_cap = total + total / 8 + 1024;
+    CK(cudaMemcpy(&nl, ta.n_large, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&chunks, ta.large_start + nl, sizeof(long long), cudaMemcpyDeviceToHost));
+    if (total > pair_cap) pair_cap = total + total / 8 + 1024;
+    if (chunks > chunk_cap) chunk_cap = chunks + chunks / 8 + 1024;
     ctx->pair_cap = (size_t)pair_cap;
+    ctx->chunk_cap = (size_t)chunk_cap;
     if (++rerun > 2) return fail(ctx, SPHG_ERR_ALLOC, "tile-pair list kept overflowing");
     goto again;
   }
   if (fp32c && (size_t)pair_cap > ctx->pair_cap) ctx->pair_cap = (size_t)pair_cap;
+  if (fp32c && (size_t)chunk_cap > ctx->chunk_cap) ctx->chunk_cap = (size_t)chunk_cap;
   if (stats) {
     stats->n_in = n;
     stats->n_mapped = (int64_t)hs.n_mapped;

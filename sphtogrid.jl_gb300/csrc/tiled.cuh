@@ -30,6 +30,11 @@ namespace sphg {
 
 enum : int { kRecFP64 = 1, kRecFallback = 2 };
 
+// Footprints above kLargeCells cells take the two-phase (multi-CTA)
+// renormalisation in chunks of kChunkCells cells.
+constexpr int64_t kLargeCells = 8192;
+constexpr int64_t kChunkCells = 4096;
+
 // Scale exponent target: the largest per-cell contribution of a channel is
 // brought to about 2^kScaleTop before it enters FP32 accumulators.
 constexpr int kScaleTop = 24;
@@ -54,6 +59,13 @@ struct TiledArgs {
   long long* tile_start;  // n_tiles + 1
   int* pairs;
   long long pair_cap;
+  // large records (two-phase renormalisation)
+  int* n_large;             // count (device counter)
+  int* large;               // record indices
+  long long* large_start;   // chunk prefix per large record (n_large + 1)
+  float4* partials;         // per chunk: compensated sum, error term, min u
+  long long chunk_cap;
+  int large_grid;
   int* exps;        // per channel max exponent (channels 0..nq-1 = Q, nq = W)
   // deterministic mode: exact int64 fixed-point tile sums
   int det;

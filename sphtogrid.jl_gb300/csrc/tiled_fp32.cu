@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(256) k_prep_count(TiledArgs A) {
           }
         }
       }
+      if ((int64_t)ni * nj * nk > kLargeCells) A.large[atomicAdd(A.n_large, 1)] = r;
       // (particle, tile) overlaps
       const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
       const int ty0 = j0 / A.tdim[1], ty1 = (j0 + nj - 1) / A.tdim[1];
@@ -125,6 +126,31 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(TiledArgs A) {
     A.tile_start[n] = part[blockDim.x - 1];
     if (part[blockDim.x - 1] > A.pair_cap) atomicOr(&A.st->flags, kFlagOverflow);
   }
+  // chunk prefix of the large records (few: a serial pass by one warp)
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nl = *A.n_large;
+    long long run = 0;
+    for (int base = 0; base < nl; base += 32) {
+      const int i = base + threadIdx.x;
+      long long c = 0;
+      if (i < nl) {
+        const int4 dm = A.dimv[A.large[i]];
+        c = ((int64_t)dm.x * dm.y * dm.z + kChunkCells - 1) / kChunkCells;
+      }
+      long long incl = c;  // inclusive warp scan
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)threadIdx.x >= o) incl += v;
+      }
+      if (i < nl) A.large_start[i] = run + incl - c;
+      run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (threadIdx.x == 0) {
+      A.large_start[nl] = run;
+      if (run > A.chunk_cap) atomicOr(&A.st->flags, kFlagOverflow);
+    }
+  }
 }
 
 }  // namespace
@@ -164,7 +190,7 @@ cudaError_t launch_tiled_fp32(int kernel, const TiledArgs& A, int num_sms, cudaS
     default: launch_norm_deposit_4(A, grid_rec, s, ev); break;
   }
   if (ev) cudaEventRecord(ev[3], s);
-  if (n_launch) *n_launch = 4;
+  if (n_launch) *n_launch = 6;
   return cudaGetLastError();
 }
 

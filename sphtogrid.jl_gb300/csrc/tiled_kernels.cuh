@@ -14,7 +14,157 @@
 namespace sphg {
 namespace tiled_detail {
 
-// K3: one warp per record: renormalisation sum, weight factor, tile lists.
+// FP32 renormalisation partial sum of record cells [f0, f1) with stride
+// `step` starting at f0 + first, compensated (TwoSum per addition), and the
+// smallest u seen.
+template <int DIMS, int KERN>
+__device__ __forceinline__ void record_sum_fp32(const float4 g, const int4 dm, int64_t f0, int64_t f1,
+                                                int first, int step, float& s, float& comp, float& umin) {
+  const int njk = dm.y * dm.z;
+  const float h = g.w, hinv = 1.0f / g.w;
+  for (int64_t f = f0 + first; f < f1; f += step) {
+    const int a = (int)(f / njk);
+    const int rr = (int)(f - (int64_t)a * njk);
+    const int b = rr / dm.z, c = rr - b * dm.z;
+    float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+    axis_f(g.x, h, a, &xd, &dx);
+    axis_f(g.y, h, b, &yd, &dy);
+    if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
+    const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
+    const float u = sqrtf(d2) * hinv;
+    umin = fminf(umin, u);
+    if (u <= 1.0f) {
+      float t, e;
+      two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
+      s = t;
+      comp += e;
+    }
+  }
+}
+
+// Compensated butterfly reduction of (s, comp) and min of umin over a warp.
+__device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& umin) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float so = __shfl_xor_sync(0xffffffffu, s, o);
+    const float co = __shfl_xor_sync(0xffffffffu, comp, o);
+    float t, e;
+    two_sum(s, so, t, e);
+    s = t;
+    comp = comp + co + e;
+    umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+  }
+}
+
+// Finishes one record with the whole warp, given its FP32 renormalisation sum
+// S and smallest u: weight factor (or the FP64 redo of ill-conditioned
+// particles), channel exponents, deterministic bounds, mass diagnostic and the
+// record's entries in the tile lists.
+template <int DIMS, int KERN>
+__device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umin, int lane, bool overflow,
+                              double& c_gm, int* emax) {
+  const int4 bx = A.box[r];
+  const int4 dm = A.dimv[r];
+  const int njk = dm.y * dm.z;
+  const int64_t F = (int64_t)dm.x * njk;
+  const int nch = A.pt.nq + 1;
+  if (A.det && lane == 0) {  // deterministic channel bounds (integer sums)
+    const double num = fabs(A.cp[r]);
+    if (num > 0.0 && num < 1e300) {
+      for (int c = 0; c < nch; ++c) {
+        const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
+        if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
+          atomicAdd(&A.bsum[c], (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c])));
+      }
+    }
+  }
+  double cpv;
+  int fl = 0;
+  double bound;  // largest per-cell weight of this particle
+  double gm;
+  if (umin > 0.9f || !(S > 0.0)) {
+    // ill-conditioned (every pixel centre near or beyond the kernel edge):
+    // the reference's FP64 arithmetic, as in the plain path
+    PrepFP64 q;
+    prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+    double s_w = 0.0, s_a = 0.0;
+    long long n_d = 0, n_t = 0;
+    for (int64_t f = lane; f < F; f += 32) {
+      const int a = (int)(f / njk);
+      const int rr = (int)(f - (int64_t)a * njk);
+      const int b = rr / dm.z, c = rr - b * dm.z;
+      double u, ar;
+      cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
+      s_a += ar;
+      n_t += 1;
+      if (u <= 1.0) {
+        s_w += kshape<KERN, double>(u) * q.knorm * ar;
+        n_d += 1;
+      }
+    }
+    s_w = warp_sum_d(s_w);
+    s_a = warp_sum_d(s_a);
+    n_d = warp_sum_ll(n_d);
+    n_t = warp_sum_ll(n_t);
+    const bool fallback = (s_w == 0.0);
+    double wpp;
+    if (fallback) {
+      n_d = n_t;
+      wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
+    } else {
+      wpp = (double)n_d / s_w;
+    }
+    cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                    : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
+    fl = kRecFP64 | (fallback ? kRecFallback : 0);
+    bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
+    gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+  } else {
+    cpv = A.cp[r] / S;
+    bound = fabs(cpv);
+    gm = A.aux[r] * S;
+  }
+  if (lane == 0) {
+    A.cp[r] = cpv;
+    if (fl) A.box[r].w = fl;
+    c_gm += gm;
+    int e;  // scale exponents per channel
+    if (bound > 0.0 && bound < 1e300) {
+      frexp(bound, &e);
+      emax[A.pt.nq] = max(emax[A.pt.nq], e);
+      for (int k = 0; k < A.pt.nq; ++k) {
+        const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+        if (qa > 0.0 && qa < 1e300) {
+          frexp(bound * qa, &e);
+          emax[k] = max(emax[k], e);
+        }
+      }
+    }
+  }
+  if (!overflow) {  // tile lists
+    const int tx0 = bx.x / A.tdim[0], tx1 = (bx.x + dm.x - 1) / A.tdim[0];
+    const int ty0 = bx.y / A.tdim[1], ty1 = (bx.y + dm.y - 1) / A.tdim[1];
+    const int tz0 = bx.z / A.tdim[2], tz1 = (bx.z + dm.z - 1) / A.tdim[2];
+    const int nty = ty1 - ty0 + 1, ntz = tz1 - tz0 + 1;
+    const int nt = (tx1 - tx0 + 1) * nty * ntz;
+    for (int t = lane; t < nt; t += 32) {
+      const int ta = t / (nty * ntz), tb = (t / ntz) % nty, tc = t % ntz;
+      const int64_t tile = ((int64_t)(tx0 + ta) * A.ntile[1] + (ty0 + tb)) * A.ntile[2] + (tz0 + tc);
+      const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
+      A.pairs[slot] = (int)r;
+    }
+  }
+}
+
+__device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int dims, double c_gm, const int* emax) {
+  if (lane == 0) {
+    if (dims == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
+    for (int c = 0; c < A.pt.nq + 1; ++c)
+      if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
+  }
+}
+
+// K3: one warp per record with a footprint of at most kLargeCells cells.
 template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
   const int lane = threadIdx.x & 31;
@@ -22,143 +172,97 @@ __global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int nrec = *A.n_rec;
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
-  const int nch = A.pt.nq + 1;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
-  for (int c = 0; c < nch; ++c) emax[c] = INT_MIN;
+  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
   for (int64_t r = wid; r < nrec; r += nw) {
-    const int4 bx = A.box[r];
     const int4 dm = A.dimv[r];
-    const float4 g = A.geo[r];
-    const int njk = dm.y * dm.z;
-    const int64_t F = (int64_t)dm.x * njk;
-    const float h = g.w, hinv = 1.0f / g.w;
-    // FP32 pass with a compensated per-lane sum
+    const int64_t F = (int64_t)dm.x * dm.y * dm.z;
+    if (F > kLargeCells) continue;  // two-phase path (k_large_partials)
     float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-    for (int64_t f = lane; f < F; f += 32) {
-      const int a = (int)(f / njk);
-      const int rr = (int)(f - (int64_t)a * njk);
-      const int b = rr / dm.z, c = rr - b * dm.z;
-      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
-      axis_f(g.x, h, a, &xd, &dx);
-      axis_f(g.y, h, b, &yd, &dy);
-      if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
-      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
-      const float u = sqrtf(d2) * hinv;
-      umin = fminf(umin, u);
-      if (u <= 1.0f) {
-        float t, e;
-        two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
-        s = t;
-        comp += e;
-      }
+    record_sum_fp32<DIMS, KERN>(A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
+    warp_reduce_comp(s, comp, umin);
+    finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax);
+  }
+  flush_stats(A, lane, DIMS, c_gm, emax);
+}
+
+// K3L phase 1: every CTA takes chunks of kChunkCells cells of the large
+// records (a persistent loop over the chunk list) and writes the chunk's
+// compensated partial sum and smallest u.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_large_partials(TiledArgs A) {
+  __shared__ float red[3][8];
+  const int nl = *A.n_large;
+  const long long total = A.large_start[nl];
+  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
+  if (overflow) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long w = blockIdx.x; w < total; w += gridDim.x) {
+    int lo = 0, hi = nl - 1;  // record whose chunk range holds w
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (A.large_start[mid] <= w) lo = mid;
+      else hi = mid - 1;
     }
-    // compensated warp reduction
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float so = __shfl_xor_sync(0xffffffffu, s, o);
-      const float co = __shfl_xor_sync(0xffffffffu, comp, o);
-      float t, e;
-      two_sum(s, so, t, e);
-      s = t;
-      comp = comp + co + e;
-      umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
-    }
-    const double S = (double)s + (double)comp;
-    if (A.det && lane == 0) {  // deterministic channel bounds (integer sums)
-      const double num = fabs(A.cp[r]);
-      if (num > 0.0 && num < 1e300) {
-        for (int c = 0; c < nch; ++c) {
-          const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
-          if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
-            atomicAdd(&A.bsum[c], (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c])));
-        }
-      }
-    }
-    double cpv;
-    int fl = 0;
-    double bound;  // largest per-cell weight of this particle
-    double gm;
-    if (umin > 0.9f || !(S > 0.0)) {
-      // ill-conditioned (every pixel centre near or beyond the kernel edge):
-      // the reference's FP64 arithmetic, as in the plain path
-      PrepFP64 q;
-      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
-      double s_w = 0.0, s_a = 0.0;
-      long long n_d = 0, n_t = 0;
-      for (int64_t f = lane; f < F; f += 32) {
-        const int a = (int)(f / njk);
-        const int rr = (int)(f - (int64_t)a * njk);
-        const int b = rr / dm.z, c = rr - b * dm.z;
-        double u, ar;
-        cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
-        s_a += ar;
-        n_t += 1;
-        if (u <= 1.0) {
-          s_w += kshape<KERN, double>(u) * q.knorm * ar;
-          n_d += 1;
-        }
-      }
-      s_w = warp_sum_d(s_w);
-      s_a = warp_sum_d(s_a);
-      n_d = warp_sum_ll(n_d);
-      n_t = warp_sum_ll(n_t);
-      const bool fallback = (s_w == 0.0);
-      double wpp;
-      if (fallback) {
-        n_d = n_t;
-        wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
-      } else {
-        wpp = (double)n_d / s_w;
-      }
-      cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
-                      : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
-      fl = kRecFP64 | (fallback ? kRecFallback : 0);
-      bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
-      gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
-    } else {
-      cpv = A.cp[r] / S;
-      bound = fabs(cpv);
-      gm = A.aux[r] * S;
-    }
+    const int64_t r = A.large[lo];
+    const int4 dm = A.dimv[r];
+    const int64_t F = (int64_t)dm.x * dm.y * dm.z;
+    const int64_t f0 = (w - A.large_start[lo]) * kChunkCells;
+    const int64_t f1 = f0 + kChunkCells < F ? f0 + kChunkCells : F;
+    float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
+    record_sum_fp32<DIMS, KERN>(A.geo[r], dm, f0, f1, threadIdx.x, blockDim.x, s, comp, umin);
+    warp_reduce_comp(s, comp, umin);
     if (lane == 0) {
-      A.cp[r] = cpv;
-      if (fl) A.box[r].w = fl;
-      c_gm += gm;
-      // scale exponents per channel
-      int e;
-      if (bound > 0.0 && bound < 1e300) {
-        frexp(bound, &e);
-        emax[A.pt.nq] = max(emax[A.pt.nq], e);
-        for (int k = 0; k < A.pt.nq; ++k) {
-          const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
-          if (qa > 0.0 && qa < 1e300) {
-            frexp(bound * qa, &e);
-            emax[k] = max(emax[k], e);
-          }
-        }
-      }
+      red[0][warp] = s;
+      red[1][warp] = comp;
+      red[2][warp] = umin;
     }
-    // tile lists
-    if (!overflow) {
-      const int tx0 = bx.x / A.tdim[0], tx1 = (bx.x + dm.x - 1) / A.tdim[0];
-      const int ty0 = bx.y / A.tdim[1], ty1 = (bx.y + dm.y - 1) / A.tdim[1];
-      const int tz0 = bx.z / A.tdim[2], tz1 = (bx.z + dm.z - 1) / A.tdim[2];
-      const int nty = ty1 - ty0 + 1, ntz = tz1 - tz0 + 1;
-      const int nt = (tx1 - tx0 + 1) * nty * ntz;
-      for (int t = lane; t < nt; t += 32) {
-        const int ta = t / (nty * ntz), tb = (t / ntz) % nty, tc = t % ntz;
-        const int64_t tile = ((int64_t)(tx0 + ta) * A.ntile[1] + (ty0 + tb)) * A.ntile[2] + (tz0 + tc);
-        const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
-        A.pairs[slot] = (int)r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float S = red[0][0], C = red[1][0], U = red[2][0];
+      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+        float t, e;
+        two_sum(S, red[0][k], t, e);
+        S = t;
+        C = C + red[1][k] + e;
+        U = fminf(U, red[2][k]);
       }
+      A.partials[w] = make_float4(S, C, U, 0.0f);
+    }
+    __syncthreads();
+  }
+}
+
+// K3L phase 2: one warp per large record sums its chunk partials in a fixed
+// order and finishes the record.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_large_finish(TiledArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nl = *A.n_large;
+  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
+  double c_gm = 0.0;
+  int emax[kMaxQ + 1];
+  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
+  if (!overflow) {
+    for (int64_t i = wid; i < nl; i += nw) {
+      const int64_t r = A.large[i];
+      float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
+      for (long long w = A.large_start[i] + lane; w < A.large_start[i + 1]; w += 32) {
+        const float4 pv = A.partials[w];
+        float t, e;
+        two_sum(s, pv.x, t, e);
+        s = t;
+        comp = comp + pv.y + e;
+        umin = fminf(umin, pv.z);
+      }
+      warp_reduce_comp(s, comp, umin);
+      finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax);
     }
   }
-  if (lane == 0) {
-    if (DIMS == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
-    for (int c = 0; c < nch; ++c)
-      if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
-  }
+  flush_stats(A, lane, DIMS, c_gm, emax);
 }
 
 // Adds one cell value to a tile accumulator (see k_deposit).
@@ -345,6 +449,8 @@ void launch_deposit_nq(const TiledArgs& A, cudaStream_t s) {
 template <int DIMS, int KERN>
 inline void launch_kern(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev) {
   k_norm_fill<DIMS, KERN><<<grid_rec, 256, 0, s>>>(A);
+  k_large_partials<DIMS, KERN><<<A.large_grid, 256, 0, s>>>(A);
+  k_large_finish<DIMS, KERN><<<A.large_grid, 256, 0, s>>>(A);
   if (ev) cudaEventRecord(ev[2], s);
   switch (DIMS == 3 ? 1 : A.pt.nq) {
     case 1: launch_deposit_nq<DIMS, KERN, 1>(A, s); break;

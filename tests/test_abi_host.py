@@ -116,3 +116,22 @@ def test_kernel_constructors(pkg):
     assert pkg.kernel_from_name("wendlandc6", 3).kind == 3
     with pytest.raises(ValueError):
         pkg.Quintic(4)
+
+
+def test_first_call_is_default_context():
+    """Creating the default context before anything else loaded the library
+    must not deadlock (fresh process; without a GPU it reports NO_DEVICE)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import __graft_entry__ as g\n"
+        "pkg = g.load_package()\n"
+        "try:\n"
+        "    pkg.default_context(0)\n"
+        "    print('context')\n"
+        "except pkg.SPHtoGridError as e:\n"
+        "    print('status', e.status)\n" % ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() in ("context", "status 10")
