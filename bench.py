@@ -215,6 +215,7 @@ def bench_gpu(args):
         o.filter = 1
         o.memspace = mem
         o.profile = profile
+        o.deterministic = int(args.deterministic and prec == "fp32c")
         return o
 
     # device-resident inputs (Julia layout: xyz contiguous per particle)
@@ -307,7 +308,8 @@ def bench_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32" if prec == "fp32c" else "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": prec, "particles": n,
+        "config": {"workload": WORKLOAD, "precision": prec, "deterministic": bool(args.deterministic),
+                   "particles": n,
                    "deposits_per_step": deposits, "maps_per_s": 1e3 / ms_step,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "working set (134 MB inputs + 60 B/particle records + 134 MB map) "
@@ -386,6 +388,8 @@ def main():
     ap.add_argument("--cpu-frac", type=float, default=1.0,
                     help="fraction of the particles the CPU baseline maps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--deterministic", action="store_true",
+                    help="bitwise reproducible int64 fixed-point tile sums")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

@@ -335,13 +335,15 @@ again:
   size_t o_acc = 0;
   if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 && !raw_out ? PD : 0) : PD * (nq + 1)) * sizeof(double));
   size_t o_box = 0, o_dim = 0, o_geo = 0, o_cp = 0, o_aux = 0, o_qv = 0, o_cnt = 0, o_start = 0,
-         o_pairs = 0, o_nrec = 0, o_exps = 0, o_large = 0, o_lstart = 0, o_part = 0;
+         o_pairs = 0, o_nrec = 0, o_exps = 0, o_large = 0, o_lstart = 0, o_part = 0, o_cpm = 0, o_cpe = 0;
   const int64_t cap = n > 0 ? n : 1;
   if (fp32c) {
     o_box = cv.take(cap * sizeof(int4));
     o_dim = cv.take(cap * sizeof(int4));
     o_geo = cv.take(cap * sizeof(float4));
     o_cp = cv.take(cap * sizeof(double));
+    o_cpm = cv.take(cap * sizeof(float));
+    o_cpe = cv.take(cap * sizeof(int));
     o_aux = cv.take(cap * sizeof(double));
     o_qv = cv.take(cap * nq * sizeof(float));
     o_cnt = cv.take((2 * ta.n_tiles + 2) * sizeof(int));  // counts, fill, record and large counters
@@ -458,6 +460,8 @@ again:
     ta.dimv = (int4*)(ws + o_dim);
     ta.geo = (float4*)(ws + o_geo);
     ta.cp = (double*)(ws + o_cp);
+    ta.cpm = (float*)(ws + o_cpm);
+    ta.cpe = (int*)(ws + o_cpe);
     ta.aux = (double*)(ws + o_aux);
     ta.qv = (float*)(ws + o_qv);
     ta.tile_count = (int*)(ws + o_cnt);

@@ -52,6 +52,8 @@ struct TiledArgs {
   int4* dimv;       // {ni, nj, nk, source particle}
   float4* geo;      // {x - iMin, y - jMin, z - kMin, h} in pixel units
   double* cp;       // K1: numerator of the weight factor; K3: the factor
+  float* cpm;       // K3: the factor as FP32 mantissa ...
+  int* cpe;         //     ... and binary exponent (cp = cpm * 2^cpe)
   double* aux;      // rho / L^3 * kernel normalisation (3D mass diagnostic)
   float* qv;        // quantities, qv[k * cap + r]
   int* tile_count;  // per tile, zeroed before K1
@@ -149,6 +151,12 @@ __device__ __forceinline__ float kshape_f(float u) {
     const float t = 1.0f - u, t2 = t * t, t4 = t2 * t2;
     return t4 * t4 * t2 * fmaf(u, fmaf(u, fmaf(u, fmaf(429.0f / 5.0f, u, 90.0f), 42.0f), 10.0f), 1.0f);
   }
+}
+
+// Distance in units of h from the squared distance (shared by the
+// renormalisation and the deposit so both see the same u).
+__device__ __forceinline__ float u_of(float d2, float hinv) {
+  return d2 > 0.0f ? d2 * rsqrtf(d2) * hinv : 0.0f;
 }
 
 // Overlap of [f - h, f + h] with local pixel a and the pixel-centre offset.

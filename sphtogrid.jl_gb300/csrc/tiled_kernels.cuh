@@ -18,26 +18,42 @@ namespace tiled_detail {
 // `step` starting at f0 + first, compensated (TwoSum per addition), and the
 // smallest u seen.
 template <int DIMS, int KERN>
+__device__ __forceinline__ void cell_sum_fp32(const float4 g, float h, float hinv, int a, int b, int c, float& s,
+                                              float& comp, float& umin) {
+  float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
+  axis_f(g.x, h, a, &xd, &dx);
+  axis_f(g.y, h, b, &yd, &dy);
+  if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
+  const float u = u_of(fmaf(xd, xd, fmaf(yd, yd, zd * zd)), hinv);
+  umin = fminf(umin, u);
+  if (u <= 1.0f) {
+    float t, e;
+    two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
+    s = t;
+    comp += e;
+  }
+}
+
+template <int DIMS, int KERN>
 __device__ __forceinline__ void record_sum_fp32(const float4 g, const int4 dm, int64_t f0, int64_t f1,
                                                 int first, int step, float& s, float& comp, float& umin) {
   const int njk = dm.y * dm.z;
   const float h = g.w, hinv = 1.0f / g.w;
-  for (int64_t f = f0 + first; f < f1; f += step) {
-    const int a = (int)(f / njk);
-    const int rr = (int)(f - (int64_t)a * njk);
-    const int b = rr / dm.z, c = rr - b * dm.z;
-    float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
-    axis_f(g.x, h, a, &xd, &dx);
-    axis_f(g.y, h, b, &yd, &dy);
-    if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
-    const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
-    const float u = sqrtf(d2) * hinv;
-    umin = fminf(umin, u);
-    if (u <= 1.0f) {
-      float t, e;
-      two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
-      s = t;
-      comp += e;
+  if (f1 + njk < (1 << 21)) {
+    // 32-bit cell index, decomposed with float reciprocals (exact here)
+    const float inv_njk = 1.0f / (float)njk, inv_nz = 1.0f / (float)dm.z;
+    for (int f = (int)f0 + first; f < (int)f1; f += step) {
+      const int a = fdiv(f, inv_njk);
+      const int rr = f - a * njk;
+      const int b = fdiv(rr, inv_nz), c = rr - b * dm.z;
+      cell_sum_fp32<DIMS, KERN>(g, h, hinv, a, b, c, s, comp, umin);
+    }
+  } else {
+    for (int64_t f = f0 + first; f < f1; f += step) {
+      const int a = (int)(f / njk);
+      const int rr = (int)(f - (int64_t)a * njk);
+      const int b = rr / dm.z, c = rr - b * dm.z;
+      cell_sum_fp32<DIMS, KERN>(g, h, hinv, a, b, c, s, comp, umin);
     }
   }
 }
@@ -78,10 +94,10 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
       }
     }
   }
-  double cpv;
+  double cpv = 0.0;
   int fl = 0;
-  double bound;  // largest per-cell weight of this particle
-  double gm;
+  double bound = 0.0;  // largest per-cell weight of this particle
+  double gm = 0.0;
   if (umin > 0.9f || !(S > 0.0)) {
     // ill-conditioned (every pixel centre near or beyond the kernel edge):
     // the reference's FP64 arithmetic, as in the plain path
@@ -119,13 +135,17 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
     fl = kRecFP64 | (fallback ? kRecFallback : 0);
     bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
     gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
-  } else {
+  } else if (lane == 0) {  // FP64 on one lane: GB300's FP64 rate is a small fraction of FP32
     cpv = A.cp[r] / S;
     bound = fabs(cpv);
     gm = A.aux[r] * S;
   }
   if (lane == 0) {
     A.cp[r] = cpv;
+    int ce = 0;
+    const float cm = (float)frexp(cpv, &ce);
+    A.cpm[r] = cm;
+    A.cpe[r] = ce;
     if (fl) A.box[r].w = fl;
     c_gm += gm;
     int e;  // scale exponents per channel
@@ -299,15 +319,19 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
   const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
   const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
   for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
-  // channel scales (powers of two)
+  // channel scales (powers of two): 2^s_shift as double for the flush
   __shared__ double s_scale[kMaxQ + 1];
+  __shared__ int s_shift[kMaxQ + 1];
   if (threadIdx.x < nch) {
+    int sh;
     if (DET) {
-      s_scale[threadIdx.x] = ldexp(1.0, fixed_exponent(A.kexp[threadIdx.x], A.bsum[threadIdx.x], *A.n_rec));
+      sh = fixed_exponent(A.kexp[threadIdx.x], A.bsum[threadIdx.x], *A.n_rec);
     } else {
       const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
-      s_scale[threadIdx.x] = e < -100000 ? 1.0 : ldexp(1.0, kScaleTop - e);
+      sh = e < -100000 ? 0 : kScaleTop - e;
     }
+    s_shift[threadIdx.x] = sh;
+    s_scale[threadIdx.x] = ldexp(1.0, sh);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -326,11 +350,12 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
     const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
     const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
     const int n = na * nb * nc;
-    const double cpv = A.cp[r];
-    float cw = __double2float_rn(cpv * scw);
+    // per-record factors in FP32: cp = cpm * 2^cpe, shifted by the channel scale
+    const float cpm = A.cpm[r];
+    const int cpe = A.cpe[r];
+    const float cw = ldexpf(cpm, cpe + s_shift[nq]);
     float cq[NQ > 0 ? NQ : kMaxQ];
-    for (int k = 0; k < nq; ++k)
-      cq[k] = __double2float_rn(cpv * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]);
+    for (int k = 0; k < nq; ++k) cq[k] = ldexpf(cpm * A.qv[(int64_t)k * A.cap + r], cpe + s_shift[k]);
     const float inv_nc = 1.0f / (float)nc, inv_nb = 1.0f / (float)nb;
     // local-frame offset of the tile origin
     const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
@@ -339,6 +364,7 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
       PrepFP64 q;
       prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
       const bool fb = (bx.w & kRecFallback) != 0;
+      const double cpv = A.cp[r];
       for (int e = lane; e < n; e += 32) {
         const int bc = fdiv(e, inv_nc);
         const int c = e - bc * nc;
@@ -371,8 +397,7 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
       axis_f(g.x, h, ia, &xd, &dx);
       axis_f(g.y, h, jb, &yd, &dy);
       if (DIMS == 3) axis_f(g.z, h, kc, &zd, &dz);
-      const float d2 = fmaf(xd, xd, fmaf(yd, yd, zd * zd));
-      const float u = sqrtf(d2) * hinv;
+      const float u = u_of(fmaf(xd, xd, fmaf(yd, yd, zd * zd)), hinv);
       if (u <= 1.0f) {
         const float gw = kshape_f<KERN>(u) * (dx * dy * dz);
         if (gw != 0.0f) {
