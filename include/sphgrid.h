@@ -210,6 +210,50 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
                  const sphg_particles *parts, const double *raw, const double *grad_out,
                  const sphg_grads *grads, void *stream);
 
+/* ---------------------------------------------------------------- batches
+ * Many maps (uneven particle counts, resolutions, quantities, kernel shapes)
+ * mapped together: one launch per phase for all maps and one persistent
+ * deposit launch over a work queue of every map's image tiles, captured once
+ * in a CUDA graph and replayed.  No counterpart in the reference, which maps
+ * one image per sphMapping call (cic_interpolation.jl:35).  Maps must use
+ * precision FP32C, device memory and centering NONE or READONLY (a replay
+ * reads the same input buffers again; refill them between launches). */
+typedef struct sphg_map_desc {
+  sphg_params par;
+  sphg_options opt;
+  sphg_particles parts;
+  double *out; /* device, sphg_output_len(&par, &opt, parts.n_q) doubles */
+} sphg_map_desc;
+
+/* Tuned quantities: 2D tile shape (16x16, 32x16 or 32x32; 3D tiles are
+ * 8x8x8), CTAs per SM of the persistent deposit, and the footprint size (in
+ * cells) above which a particle's renormalisation is split across CTAs. */
+typedef struct sphg_batch_tuning {
+  int32_t tile_x, tile_y;
+  int32_t ctas_per_sm;
+  int32_t large_cells;
+  float tuned_ms;      /* autotuned: time of one eager run of the chosen plan */
+  int32_t reserved[3];
+} sphg_batch_tuning;
+
+typedef struct sphg_batch sphg_batch;
+
+/* Plans a batch: sizes the intermediate lists by mapping once, autotunes when
+ * `tuning` is NULL (trying tile shapes, CTAs per SM and large-footprint
+ * thresholds), and captures the pipeline in a CUDA graph.  The outputs hold
+ * valid maps on return. */
+int sphg_batch_create(sphg_context *ctx, int32_t n_maps, const sphg_map_desc *maps,
+                      const sphg_batch_tuning *tuning, sphg_batch **out);
+/* Replays the captured graph on `stream` (NULL: the batch's own stream). */
+int sphg_batch_launch(sphg_batch *batch, void *stream);
+/* Waits for the last launch, checks every map's status (growing the lists and
+ * re-capturing if the inputs outgrew them) and fills `stats[n_maps]` (may be
+ * NULL). */
+int sphg_batch_wait(sphg_batch *batch, sphg_stats *stats);
+int sphg_batch_get_tuning(const sphg_batch *batch, sphg_batch_tuning *out);
+const char *sphg_batch_last_error(const sphg_batch *batch);
+int sphg_batch_destroy(sphg_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

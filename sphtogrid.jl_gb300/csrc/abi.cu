@@ -118,6 +118,15 @@ bool valid_dtype(int dt) { return dt == SPHG_F32 || dt == SPHG_F64; }
 
 }  // namespace
 
+namespace sphg {
+int context_device(sphg_context* ctx) { return ctx->device; }
+int context_num_sms(sphg_context* ctx) { return ctx->num_sms; }
+void set_context_error(sphg_context* ctx, const std::string& msg) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->last_error = msg;
+}
+}  // namespace sphg
+
 extern "C" {
 
 int sphg_abi_version(void) { return SPHG_ABI_VERSION; }
@@ -480,6 +489,8 @@ again:
     ta.partials = (float4*)(ws + o_part);
     ta.chunk_cap = chunk_cap;
     ta.large_grid = ctx->num_sms * 4;
+    ta.kern = opt->kernel;
+    ta.large_cells = (int)sphg::kLargeCells;
     ta.st = ctx->d_status;
     ta.out = dout;
     ta.mode = raw_out ? 1 : (dims == 3 ? 2 : 0);

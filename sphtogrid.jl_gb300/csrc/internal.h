@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
+#include "../../include/sphgrid.h"
 #include "common.cuh"
 #include "tiled.cuh"
 
@@ -20,6 +22,11 @@ void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& m
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s);
 void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one, double* out,
                       int num_sms, cudaStream_t s);
+
+// Context accessors for the other translation units (abi.cu).
+int context_device(sphg_context* ctx);
+int context_num_sms(sphg_context* ctx);
+void set_context_error(sphg_context* ctx, const std::string& msg);
 
 // Tile shape and tile counts of the FP32-compensated path.
 void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles);

@@ -30,8 +30,9 @@ namespace sphg {
 
 enum : int { kRecFP64 = 1, kRecFallback = 2 };
 
-// Footprints above kLargeCells cells take the two-phase (multi-CTA)
-// renormalisation in chunks of kChunkCells cells.
+// Footprints above kLargeCells cells (the default of TiledArgs::large_cells)
+// take the two-phase (multi-CTA) renormalisation in chunks of kChunkCells
+// cells.
 constexpr int64_t kLargeCells = 8192;
 constexpr int64_t kChunkCells = 4096;
 
@@ -42,6 +43,8 @@ constexpr int kScaleTop = 24;
 struct TiledArgs {
   DevParticles pt;
   DevMapParams mp;
+  int kern;         // SPHKernels shape (used where the shape is a runtime value)
+  int large_cells;  // footprints above this many cells take the two-phase path
   DevMapParams mp_re;  // re-derivation after K1 (positions already centred in place)
   int tdim[3];      // tile extent per axis (1 on the unused 2D axis)
   int ntile[3];     // tiles per axis
@@ -157,6 +160,32 @@ __device__ __forceinline__ float kshape_f(float u) {
 // renormalisation and the deposit so both see the same u).
 __device__ __forceinline__ float u_of(float d2, float hinv) {
   return d2 > 0.0f ? d2 * rsqrtf(d2) * hinv : 0.0f;
+}
+
+// Kernel shape with the shape chosen at compile time (KERN >= 0) or at run
+// time (KERN < 0: `kern`, uniform across a warp).
+template <int KERN>
+__device__ __forceinline__ float shape_f(int kern, float u) {
+  if (KERN >= 0) return kshape_f<(KERN < 0 ? 0 : KERN)>(u);
+  switch (kern) {
+    case 0: return kshape_f<0>(u);
+    case 1: return kshape_f<1>(u);
+    case 2: return kshape_f<2>(u);
+    case 3: return kshape_f<3>(u);
+    default: return kshape_f<4>(u);
+  }
+}
+
+template <int KERN>
+__device__ __forceinline__ double shape_d(int kern, double u) {
+  if (KERN >= 0) return kshape<(KERN < 0 ? 0 : KERN), double>(u);
+  switch (kern) {
+    case 0: return kshape<0, double>(u);
+    case 1: return kshape<1, double>(u);
+    case 2: return kshape<2, double>(u);
+    case 3: return kshape<3, double>(u);
+    default: return kshape<4, double>(u);
+  }
 }
 
 // Overlap of [f - h, f + h] with local pixel a and the pixel-centre offset.

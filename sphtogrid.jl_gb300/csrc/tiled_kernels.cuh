@@ -14,12 +14,158 @@
 namespace sphg {
 namespace tiled_detail {
 
+// K1 body: this CTA's threads take particles base0 + threadIdx.x, then
+// every `stride` further (a whole CTA enters each iteration together).
+template <int DIMS>
+__device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long c_mapped = 0, c_dep = 0;
+  double c_pm = 0.0;
+  unsigned flags = 0;
+  int kmax[kMaxQ + 1];
+  if (A.det)
+    for (int c = 0; c <= A.pt.nq; ++c) kmax[c] = INT_MIN;
+  for (int64_t base = base0; base < A.pt.n; base += stride) {
+    const int64_t p = base + threadIdx.x;
+    PrepFP64 q;
+    int state = kPrepSkip;
+    if (p < A.pt.n) state = prep_particle_fp64<DIMS>(A.pt, A.mp, p, true, &q);
+    if (state == kPrepNonFinite) flags |= kFlagNonFinite;
+    int ni = 0, nj = 0, nk = 0;
+    if (state == kPrepMapped) {
+      ni = (int)(q.hi[0] - q.lo[0] + 1);
+      nj = (int)(q.hi[1] - q.lo[1] + 1);
+      nk = (int)(q.hi[2] - q.lo[2] + 1);
+      c_mapped += 1;
+      c_dep += (unsigned long long)ni * nj * nk;
+      c_pm += q.m_in;
+    }
+    const bool rec = state == kPrepMapped && ni > 0 && nj > 0 && nk > 0;
+    // warp-aggregated slot allocation
+    const unsigned bal = __ballot_sync(0xffffffffu, rec);
+    int slot0 = 0;
+    if (bal) {
+      const int leader = __ffs(bal) - 1;
+      if (lane == leader) slot0 = atomicAdd(A.n_rec, __popc(bal));
+      slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+    }
+    if (rec) {
+      const int r = slot0 + __popc(bal & lanemask_lt());
+      const int i0 = (int)q.lo[0], j0 = (int)q.lo[1], k0 = (int)q.lo[2];
+      A.box[r] = make_int4(i0, j0, k0, 0);
+      A.dimv[r] = make_int4(ni, nj, nk, (int)p);
+      A.geo[r] = make_float4(__double2float_rn(q.x - (double)i0), __double2float_rn(q.y - (double)j0),
+                             DIMS == 3 ? __double2float_rn(q.z - (double)k0) : 0.0f,
+                             __double2float_rn(q.hsml));
+      // weight factor numerator: area*w*dz (cic_2D.jl:187-188) / vol*w*L (cic_3D.jl:168-169)
+      A.cp[r] = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
+      A.aux[r] = q.rho_in * q.knorm / (A.mp.L * A.mp.L * A.mp.L);
+      for (int k = 0; k < A.pt.nq; ++k)
+        A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
+            : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
+      if (A.det) {  // exponent of the particle's total per channel
+        const double num = fabs(A.cp[r]);
+        int e;
+        if (num > 0.0 && num < 1e300) {
+          frexp(num, &e);
+          kmax[A.pt.nq] = max(kmax[A.pt.nq], e);
+          for (int k = 0; k < A.pt.nq; ++k) {
+            const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+            if (qa > 0.0 && qa < 1e300) {
+              frexp(num * qa, &e);
+              kmax[k] = max(kmax[k], e);
+            }
+          }
+        }
+      }
+      if ((int64_t)ni * nj * nk > A.large_cells) A.large[atomicAdd(A.n_large, 1)] = r;
+      // (particle, tile) overlaps
+      const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
+      const int ty0 = j0 / A.tdim[1], ty1 = (j0 + nj - 1) / A.tdim[1];
+      const int tz0 = k0 / A.tdim[2], tz1 = (k0 + nk - 1) / A.tdim[2];
+      for (int tx = tx0; tx <= tx1; ++tx)
+        for (int ty = ty0; ty <= ty1; ++ty)
+          for (int tz = tz0; tz <= tz1; ++tz)
+            atomicAdd(&A.tile_count[((int64_t)tx * A.ntile[1] + ty) * A.ntile[2] + tz], 1);
+    }
+  }
+  c_pm = warp_sum_d(c_pm);
+  c_mapped = (unsigned long long)warp_sum_ll((long long)c_mapped);
+  c_dep = (unsigned long long)warp_sum_ll((long long)c_dep);
+  flags = __reduce_or_sync(0xffffffffu, flags);
+  if (A.det)  // one atomic per warp and channel
+    for (int c = 0; c <= A.pt.nq; ++c) {
+      const int km = __reduce_max_sync(0xffffffffu, kmax[c]);
+      if (lane == 0 && km != INT_MIN) atomicMax(&A.kexp[c], km);
+    }
+  if (lane == 0) {
+    if (c_mapped) {
+      atomicAdd(&A.st->n_mapped, c_mapped);
+      atomicAdd(&A.st->deposits, c_dep);
+      atomicAdd(&A.st->particle_mass, c_pm);
+    }
+    if (flags) atomicOr(&A.st->flags, flags);
+  }
+}
+
+// K2 body: exclusive scan of the tile counts by one CTA of 1024 threads.
+__device__ inline void scan_tiles(const TiledArgs& A, long long* part) {
+  const int64_t n = A.n_tiles;
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
+  long long s = 0;
+  for (int64_t i = b; i < e; ++i) s += A.tile_count[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // Hillis-Steele inclusive scan
+    long long v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int64_t i = b; i < e; ++i) {
+    A.tile_start[i] = run;
+    run += A.tile_count[i];
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    A.tile_start[n] = part[blockDim.x - 1];
+    if (part[blockDim.x - 1] > A.pair_cap) atomicOr(&A.st->flags, kFlagOverflow);
+  }
+  // chunk prefix of the large records (few: a serial pass by one warp)
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nl = *A.n_large;
+    long long run = 0;
+    for (int base = 0; base < nl; base += 32) {
+      const int i = base + threadIdx.x;
+      long long c = 0;
+      if (i < nl) {
+        const int4 dm = A.dimv[A.large[i]];
+        c = ((int64_t)dm.x * dm.y * dm.z + kChunkCells - 1) / kChunkCells;
+      }
+      long long incl = c;  // inclusive warp scan
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)threadIdx.x >= o) incl += v;
+      }
+      if (i < nl) A.large_start[i] = run + incl - c;
+      run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (threadIdx.x == 0) {
+      A.large_start[nl] = run;
+      if (run > A.chunk_cap) atomicOr(&A.st->flags, kFlagOverflow);
+    }
+  }
+}
+
+
 // FP32 renormalisation partial sum of record cells [f0, f1) with stride
 // `step` starting at f0 + first, compensated (TwoSum per addition), and the
 // smallest u seen.
 template <int DIMS, int KERN>
-__device__ __forceinline__ void cell_sum_fp32(const float4 g, float h, float hinv, int a, int b, int c, float& s,
-                                              float& comp, float& umin) {
+__device__ __forceinline__ void cell_sum_fp32(int kern, const float4 g, float h, float hinv, int a, int b, int c,
+                                              float& s, float& comp, float& umin) {
   float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
   axis_f(g.x, h, a, &xd, &dx);
   axis_f(g.y, h, b, &yd, &dy);
@@ -28,14 +174,14 @@ __device__ __forceinline__ void cell_sum_fp32(const float4 g, float h, float hin
   umin = fminf(umin, u);
   if (u <= 1.0f) {
     float t, e;
-    two_sum(s, kshape_f<KERN>(u) * (dx * dy * dz), t, e);
+    two_sum(s, shape_f<KERN>(kern, u) * (dx * dy * dz), t, e);
     s = t;
     comp += e;
   }
 }
 
 template <int DIMS, int KERN>
-__device__ __forceinline__ void record_sum_fp32(const float4 g, const int4 dm, int64_t f0, int64_t f1,
+__device__ __forceinline__ void record_sum_fp32(int kern, const float4 g, const int4 dm, int64_t f0, int64_t f1,
                                                 int first, int step, float& s, float& comp, float& umin) {
   const int njk = dm.y * dm.z;
   const float h = g.w, hinv = 1.0f / g.w;
@@ -46,14 +192,14 @@ __device__ __forceinline__ void record_sum_fp32(const float4 g, const int4 dm, i
       const int a = fdiv(f, inv_njk);
       const int rr = f - a * njk;
       const int b = fdiv(rr, inv_nz), c = rr - b * dm.z;
-      cell_sum_fp32<DIMS, KERN>(g, h, hinv, a, b, c, s, comp, umin);
+      cell_sum_fp32<DIMS, KERN>(kern, g, h, hinv, a, b, c, s, comp, umin);
     }
   } else {
     for (int64_t f = f0 + first; f < f1; f += step) {
       const int a = (int)(f / njk);
       const int rr = (int)(f - (int64_t)a * njk);
       const int b = rr / dm.z, c = rr - b * dm.z;
-      cell_sum_fp32<DIMS, KERN>(g, h, hinv, a, b, c, s, comp, umin);
+      cell_sum_fp32<DIMS, KERN>(kern, g, h, hinv, a, b, c, s, comp, umin);
     }
   }
 }
@@ -78,19 +224,19 @@ __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& u
 // record's entries in the tile lists.
 template <int DIMS, int KERN>
 __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umin, int lane, bool overflow,
-                              double& c_gm, int* emax) {
+                              double& c_gm, int* emax, unsigned long long* bacc) {
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
   const int njk = dm.y * dm.z;
   const int64_t F = (int64_t)dm.x * njk;
   const int nch = A.pt.nq + 1;
-  if (A.det && lane == 0) {  // deterministic channel bounds (integer sums)
+  if (A.det && lane == 0) {  // deterministic channel bounds (integer sums, flushed per warp)
     const double num = fabs(A.cp[r]);
     if (num > 0.0 && num < 1e300) {
       for (int c = 0; c < nch; ++c) {
         const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
         if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
-          atomicAdd(&A.bsum[c], (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c])));
+          bacc[c] += (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c]));
       }
     }
   }
@@ -114,7 +260,7 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
       s_a += ar;
       n_t += 1;
       if (u <= 1.0) {
-        s_w += kshape<KERN, double>(u) * q.knorm * ar;
+        s_w += shape_d<KERN>(A.kern, u) * q.knorm * ar;
         n_d += 1;
       }
     }
@@ -176,49 +322,60 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
   }
 }
 
-__device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int dims, double c_gm, const int* emax) {
+__device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int dims, double c_gm, const int* emax,
+                                            const unsigned long long* bacc) {
   if (lane == 0) {
     if (dims == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
-    for (int c = 0; c < A.pt.nq + 1; ++c)
+    for (int c = 0; c < A.pt.nq + 1; ++c) {
       if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
+      if (bacc[c]) atomicAdd(&A.bsum[c], bacc[c]);
+    }
   }
 }
 
-// K3: one warp per record with a footprint of at most kLargeCells cells.
+// K3 body: the warp `wid` of `nw` takes the records with a footprint of at
+// most large_cells cells.
 template <int DIMS, int KERN>
-__global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+__device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int lane) {
   const int nrec = *A.n_rec;
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
-  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
+  unsigned long long bacc[kMaxQ + 1];
+  for (int c = 0; c <= A.pt.nq; ++c) {
+    emax[c] = INT_MIN;
+    bacc[c] = 0ull;
+  }
   for (int64_t r = wid; r < nrec; r += nw) {
     const int4 dm = A.dimv[r];
     const int64_t F = (int64_t)dm.x * dm.y * dm.z;
-    if (F > kLargeCells) continue;  // two-phase path (k_large_partials)
+    if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
     float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-    record_sum_fp32<DIMS, KERN>(A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
+    record_sum_fp32<DIMS, KERN>(A.kern, A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
     warp_reduce_comp(s, comp, umin);
-    finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax);
+    finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax, bacc);
   }
-  flush_stats(A, lane, DIMS, c_gm, emax);
+  flush_stats(A, lane, DIMS, c_gm, emax, bacc);
+}
+
+// K3: one warp per small record.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
+  norm_records<DIMS, KERN>(A, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                           ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
 }
 
 // K3L phase 1: every CTA takes chunks of kChunkCells cells of the large
 // records (a persistent loop over the chunk list) and writes the chunk's
 // compensated partial sum and smallest u.
 template <int DIMS, int KERN>
-__global__ void __launch_bounds__(256) k_large_partials(TiledArgs A) {
-  __shared__ float red[3][8];
+__device__ void large_partials(const TiledArgs& A, int64_t bid, int64_t nblocks, float (*red)[8]) {
   const int nl = *A.n_large;
   const long long total = A.large_start[nl];
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   if (overflow) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (long long w = blockIdx.x; w < total; w += gridDim.x) {
+  for (long long w = bid; w < total; w += nblocks) {
     int lo = 0, hi = nl - 1;  // record whose chunk range holds w
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -231,7 +388,7 @@ __global__ void __launch_bounds__(256) k_large_partials(TiledArgs A) {
     const int64_t f0 = (w - A.large_start[lo]) * kChunkCells;
     const int64_t f1 = f0 + kChunkCells < F ? f0 + kChunkCells : F;
     float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-    record_sum_fp32<DIMS, KERN>(A.geo[r], dm, f0, f1, threadIdx.x, blockDim.x, s, comp, umin);
+    record_sum_fp32<DIMS, KERN>(A.kern, A.geo[r], dm, f0, f1, threadIdx.x, blockDim.x, s, comp, umin);
     warp_reduce_comp(s, comp, umin);
     if (lane == 0) {
       red[0][warp] = s;
@@ -254,18 +411,25 @@ __global__ void __launch_bounds__(256) k_large_partials(TiledArgs A) {
   }
 }
 
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_large_partials(TiledArgs A) {
+  __shared__ float red[3][8];
+  large_partials<DIMS, KERN>(A, blockIdx.x, gridDim.x, red);
+}
+
 // K3L phase 2: one warp per large record sums its chunk partials in a fixed
 // order and finishes the record.
 template <int DIMS, int KERN>
-__global__ void __launch_bounds__(256) k_large_finish(TiledArgs A) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+__device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int lane) {
   const int nl = *A.n_large;
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
-  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
+  unsigned long long bacc[kMaxQ + 1];
+  for (int c = 0; c <= A.pt.nq; ++c) {
+    emax[c] = INT_MIN;
+    bacc[c] = 0ull;
+  }
   if (!overflow) {
     for (int64_t i = wid; i < nl; i += nw) {
       const int64_t r = A.large[i];
@@ -279,10 +443,16 @@ __global__ void __launch_bounds__(256) k_large_finish(TiledArgs A) {
         umin = fminf(umin, pv.z);
       }
       warp_reduce_comp(s, comp, umin);
-      finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax);
+      finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax, bacc);
     }
   }
-  flush_stats(A, lane, DIMS, c_gm, emax);
+  flush_stats(A, lane, DIMS, c_gm, emax, bacc);
+}
+
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256) k_large_finish(TiledArgs A) {
+  large_finish<DIMS, KERN>(A, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                           ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
 }
 
 // Adds one cell value to a tile accumulator (see k_deposit).
@@ -305,15 +475,13 @@ __device__ __forceinline__ double cell_value(const float* hi, const float* lo, c
 // (bitwise reproducible) instead of TwoSum-compensated FP32 (hi, lo) pairs;
 // both use 8 bytes per channel and tile pixel.
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-__global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
+__device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw) {
   constexpr int TV = TX * TY * TZ;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nq = NQ > 0 ? NQ : A.pt.nq;
   const int nch = nq + 1;
   float* hi = (float*)smem_raw;             // [nch][TV]
   float* lo = hi + nch * TV;                // [nch][TV]
   unsigned long long* fx = (unsigned long long*)smem_raw;  // DET: [nch][TV]
-  const int64_t t = blockIdx.x;
   const int tz = (int)(t % A.ntile[2]);
   const int ty = (int)((t / A.ntile[2]) % A.ntile[1]);
   const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
@@ -373,7 +541,7 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
         const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
         double u, ar;
         cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
-        const double wk = fb ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * q.knorm : 0.0);
+        const double wk = fb ? 1.0 : (u <= 1.0 ? shape_d<KERN>(A.kern, u) * q.knorm : 0.0);
         const double pw = wk * ar * cpv;
         if (pw != 0.0) {
           const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
@@ -399,7 +567,7 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
       if (DIMS == 3) axis_f(g.z, h, kc, &zd, &dz);
       const float u = u_of(fmaf(xd, xd, fmaf(yd, yd, zd * zd)), hinv);
       if (u <= 1.0f) {
-        const float gw = kshape_f<KERN>(u) * (dx * dy * dz);
+        const float gw = shape_f<KERN>(A.kern, u) * (dx * dy * dz);
         if (gw != 0.0f) {
           const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
           acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
@@ -450,6 +618,13 @@ __global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
       }
     }
   }
+  __syncthreads();  // the shared accumulators are reused by the next tile
+}
+
+template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
+__global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw);
 }
 
 template <int DIMS, int KERN, int NQ, bool DET>

@@ -98,3 +98,33 @@ def differentiable_2d(N=2 ** 20, npix=512, seed=0, dtype=np.float64):
     """Adjoint workload: as ``uniform_2d`` mapped to 512^2 with WendlandC4."""
     d = uniform_2d(N=N, npix=npix, kernel="wendlandc4", seed=seed, dtype=dtype)
     return d
+
+
+def batched_2d(n_maps=96, seed=0, dtype=np.float32, n_min=10_000, n_max=2_000_000,
+               sizes=(128, 256, 512, 1024)):
+    """Batched workload: independent 2D maps with particle counts lognormal
+    between n_min and n_max, Npixels drawn from `sizes`, 1-4 quantities (rho,
+    temperature lognormal median 1e6, a velocity component Gaussian sigma 300,
+    magnetic-field magnitude lognormal), Quintic and WendlandC4 mixed;
+    positions and hsml as ``uniform_2d``.  Returns a list of map dicts."""
+    rng = np.random.default_rng(seed)
+    mu = 0.5 * (math.log(n_min) + math.log(n_max))
+    sig = (math.log(n_max) - math.log(n_min)) / 4.0
+    maps = []
+    for _ in range(n_maps):
+        N = int(np.clip(round(math.exp(rng.normal(mu, sig))), n_min, n_max))
+        P = int(rng.choice(sizes))
+        nq = int(rng.integers(1, 5))
+        kernel = str(rng.choice(["quintic", "wendlandc4"]))
+        pos = rng.random((3, N))
+        hsml = np.clip(np.exp(np.log(0.01) + 0.5 * rng.standard_normal(N)), 0.002, 0.1)
+        rho = rng.uniform(0.5, 2.0, N)
+        rows = [rho, np.exp(np.log(1e6) + rng.standard_normal(N)), 300.0 * rng.standard_normal(N),
+                np.exp(np.log(1e-6) + rng.standard_normal(N))]
+        q = np.stack(rows[:nq]) if nq > 1 else rows[0]
+        d = {"pos": _julia_pos(pos.astype(dtype)), "hsml": hsml.astype(dtype),
+             "mass": np.full(N, 1.0 / N, dtype=dtype), "rho": rho.astype(dtype),
+             "bin_q": np.ascontiguousarray(q.astype(dtype)), "weights": rho.astype(dtype),
+             "limits": (0.0, 1.0), "npix": P, "kernel": kernel, "dims": 2}
+        maps.append(d)
+    return maps

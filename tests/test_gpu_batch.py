@@ -1,0 +1,106 @@
+"""Batched maps (one persistent deposit over all maps' tiles, CUDA graph,
+autotuner) against the single-map path and the oracle."""
+import numpy as np
+import pytest
+
+from conftest import rel_linf
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _maps(seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, (n, P, nq, kern, dims) in enumerate([(3000, 48, 1, "quintic", 2), (12000, 64, 3, "wendlandc4", 2),
+                                                (500, 32, 2, "cubic", 2), (20000, 40, 4, "wendlandc4", 2),
+                                                (900, 24, 1, "wendlandc6", 3), (1, 16, 1, "cubic", 2),
+                                                (6000, 37, 2, "quintic", 2)]):
+        pos = np.asfortranarray(rng.random((3, n)).astype(np.float32))
+        hsml = np.clip(np.exp(np.log(0.02) + 0.6 * rng.standard_normal(n)), 0.002, 0.3).astype(np.float32)
+        rho = rng.uniform(0.5, 2.0, n).astype(np.float32)
+        q = (rng.uniform(0.5, 2.0, (nq, n)) if nq > 1 else rng.uniform(0.5, 2.0, n)).astype(np.float32)
+        out.append(dict(pos=pos, hsml=hsml, m=np.full(n, 1.0 / n, np.float32), rho=rho, q=q, w=rho.copy(),
+                        P=P, kernel=kern, dims=dims))
+    return out
+
+
+def _dev(a):
+    return torch.tensor(np.ascontiguousarray(a), device="cuda")
+
+
+def _specs(gpu, maps):
+    from sphtogrid_gb300.batch import MapSpec
+    specs, host = [], []
+    for d in maps:
+        par = gpu.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["P"])
+        tpos = _dev(d["pos"].T).T
+        ts = [_dev(d[k]) for k in ("hsml", "m", "rho", "q", "w")]
+        specs.append(MapSpec(tpos, *ts, param=par, kernel=gpu.kernel_from_name(d["kernel"], d["dims"]),
+                             dimensions=d["dims"]))
+        host.append((par, tpos, ts))
+    return specs, host
+
+
+def _single(gpu, d, par, deterministic=False):
+    return gpu.sphMapping(d["pos"].copy(order="F"), d["hsml"], d["m"], d["rho"], d["q"], d["w"],
+                          param=par, kernel=gpu.kernel_from_name(d["kernel"], d["dims"]),
+                          dimensions=d["dims"], precision="fp32c", deterministic=deterministic,
+                          show_progress=False)
+
+
+def test_batch_matches_single_maps(gpu, oracle):
+    from sphtogrid_gb300.batch import SPHBatch
+    maps = _maps(1)
+    specs, host = _specs(gpu, maps)
+    b = SPHBatch(specs)  # autotuned
+    tun = b.tuning
+    assert (tun["tile_x"], tun["tile_y"]) in ((16, 16), (32, 16), (32, 32))
+    assert tun["ctas_per_sm"] >= 1 and tun["tuned_ms"] > 0
+    b.launch()
+    stats = b.wait()
+    for i, d in enumerate(maps):
+        got = b.image(i).cpu().numpy()
+        ref = _single(gpu, d, host[i][0])
+        assert got.shape == ref.shape
+        assert rel_linf(got, ref, 1e-9) <= 1e-6, i
+        opar = oracle.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["P"])
+        _, info = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["m"], d["rho"], d["q"],
+                                     d["w"], param=opar, kernel=d["kernel"], dimensions=d["dims"])
+        assert stats[i]["deposits"] == info["deposits"]
+        assert stats[i]["n_launches"] == 6
+    b.close()
+
+
+def test_batch_deterministic_is_bitwise_single(gpu):
+    from sphtogrid_gb300.batch import SPHBatch
+    maps = _maps(2)
+    specs, host = _specs(gpu, maps)
+    b = SPHBatch(specs, deterministic=True, tuning=(32, 16, 4, 8192))
+    b.launch()
+    b.wait()
+    for i, d in enumerate(maps):
+        got = b.image(i).cpu().numpy()
+        ref = _single(gpu, d, host[i][0], deterministic=True)
+        assert np.array_equal(got, ref), i
+    b.close()
+
+
+def test_batch_relaunch_sees_new_inputs(gpu):
+    from sphtogrid_gb300.batch import SPHBatch
+    maps = _maps(3)[:4]
+    specs, host = _specs(gpu, maps)
+    b = SPHBatch(specs, tuning=(16, 16, 4, 8192))
+    b.launch()
+    b.wait()
+    first = [b.image(i).clone() for i in range(len(maps))]
+    for par, tpos, ts in host:
+        ts[3].mul_(2.0)  # Bin_Quant doubled in place: Q/W doubles
+    torch.cuda.synchronize()
+    for _ in range(3):
+        b.launch()
+    b.wait()
+    for i in range(len(maps)):
+        got = b.image(i)
+        assert torch.allclose(got, 2.0 * first[i], rtol=1e-6, atol=1e-12 * float(first[i].abs().max()))
+    b.close()

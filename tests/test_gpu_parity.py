@@ -61,8 +61,9 @@ def _compare(gpu, oracle, case, P, dims, kernel, kdim=None, precision="fp64", to
     img, st = gpu.sphMapping(pos_g, hsml, m, rho, q, w, param=par,
                              kernel=gpu.kernel_from_name(kernel, kdim), dimensions=dims,
                              precision=precision, show_progress=False, return_stats=True, **kw)
+    okw = {k: v for k, v in kw.items() if k != "deterministic"}  # GPU-only option
     ref, info = oracle.sph_mapping(pos_o, hsml, m, rho, q, w, param=opar, kernel=kernel,
-                                   kernel_dim=kdim, dimensions=dims, copy_pos=False, **kw)
+                                   kernel_dim=kdim, dimensions=dims, copy_pos=False, **okw)
     # in-place centring is bitwise the reference's (filter_shift.jl:15)
     assert np.array_equal(pos_g, pos_o)
     assert st["deposits"] == info["deposits"]
@@ -70,7 +71,7 @@ def _compare(gpu, oracle, case, P, dims, kernel, kdim=None, precision="fp64", to
     if precision == "fp64" or img.size == 0:
         err = rel_linf(img, ref, FLOOR)
     else:
-        wmask = _weight_mask(oracle, case, opar, dims, kernel, kdim, img.shape, **kw)
+        wmask = _weight_mask(oracle, case, opar, dims, kernel, kdim, img.shape, **okw)
         err = rel_linf(img[wmask], ref[wmask], FLOOR) if wmask.any() else 0.0
     assert err <= limit, f"rel L-inf {err:.3e}"
     return img, ref, st, info
