@@ -210,6 +210,37 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
                  const sphg_particles *parts, const double *raw, const double *grad_out,
                  const sphg_grads *grads, void *stream);
 
+/* ------------------------------------------------------- no-allocation map
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code running inside a host application that owns all device memory
+ * through its own pool (an in-situ map under a fixed memory budget, a plugin
+ * whose host forbids allocations during a time step), where cudaMalloc and
+ * cudaFree either fail or stall the device mid-step.
+ *
+ * sphg_map_noalloc maps like sphg_map with precision FP32C, but needs no
+ * context and calls no cudaMalloc, cudaFree or allocating library routine.
+ * Its scratch (particle records, tile lists, the (particle, tile) overlap
+ * list, the status word) is one static device array of
+ * SPHG_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
+ * the process exits.  Limits: records take (72 + 4 n_q) bytes per input
+ * particle and the overlap list 4 bytes per (particle, tile) pair, so a few
+ * hundred thousand particles fit; larger calls return SPHG_ERR_ARG (before
+ * any work) or SPHG_ERR_ALLOC (overlap list full) -- use sphg_map for them.
+ *
+ * - Device memory only (opt->memspace = SPHG_MEM_DEVICE); runs on the
+ *   caller's current device and `stream` (NULL: the legacy default stream)
+ *   and returns when the map is complete.
+ * - The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ * - Every call on a device shares the one array and clears what it
+ *   accumulates into; calls that overlap on the GPU (other streams or host
+ *   threads without ordering between them) race and corrupt each other.
+ * - Errors: sphg_last_error(NULL) gives the message (per host thread). */
+#define SPHG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+int sphg_map_noalloc(const sphg_params *par, const sphg_options *opt, const sphg_particles *parts,
+                     double *out, void *stream, sphg_stats *stats);
+
 /* ---------------------------------------------------------------- batches
  * Many maps (uneven particle counts, resolutions, quantities, kernel shapes)
  * mapped together: one launch per phase for all maps and one persistent

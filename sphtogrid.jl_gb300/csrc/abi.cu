@@ -125,6 +125,7 @@ void set_context_error(sphg_context* ctx, const std::string& msg) {
   std::lock_guard<std::mutex> lk(ctx->mu);
   ctx->last_error = msg;
 }
+void set_thread_error(const std::string& msg) { g_error = msg; }
 }  // namespace sphg
 
 extern "C" {

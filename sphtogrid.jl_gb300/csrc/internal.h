@@ -27,6 +27,8 @@ void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one
 int context_device(sphg_context* ctx);
 int context_num_sms(sphg_context* ctx);
 void set_context_error(sphg_context* ctx, const std::string& msg);
+// Message returned by sphg_last_error(NULL) on this host thread.
+void set_thread_error(const std::string& msg);
 
 // Tile shape and tile counts of the FP32-compensated path.
 void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_tiles);
