@@ -198,6 +198,13 @@ int sphg_map(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
 int sphg_reduce(sphg_context *ctx, const sphg_params *par, const sphg_options *opt, int32_t n_q,
                 const double *raw, double *out, void *stream);
 
+/* distributed_cic_map's summation of sub-file maps
+ * (src/distributed_mapping/cic.jl:55-78): adds the finite entries of the raw
+ * accumulator `part` into `sum` (both `len` doubles, device memory); NaN and
+ * Inf entries are skipped as in the reference.  Reduce the sum with
+ * sphg_reduce. */
+int sphg_accumulate(sphg_context *ctx, int64_t len, const double *part, double *sum, void *stream);
+
 /* Adjoint of sphg_map (no counterpart in the reference, which has no
  * derivatives): given the forward's raw accumulator `raw` ((P^D, Nq+1), from
  * raw_accumulator = 1) and dL/d(output) `grad_out` in the layout of the

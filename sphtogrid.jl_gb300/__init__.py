@@ -17,6 +17,12 @@ def __getattr__(name):
     if name in ("sph_map_differentiable", "SPHMapFunction"):
         from . import autograd
         return getattr(autograd, name)
+    if name == "distributed_cic_map":
+        from . import distributed
+        return distributed.distributed_cic_map
+    if name == "SPHBatch" or name == "MapSpec":
+        from . import batch
+        return getattr(batch, name)
     raise AttributeError(name)
 
 __all__ = ["mappingParameters", "MappingParameters", "sphMapping", "Cubic", "Quintic",

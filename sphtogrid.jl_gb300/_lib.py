@@ -114,6 +114,14 @@ class SphgGrads(C.Structure):
     ]
 
 
+def stream_handle(stream) -> C.c_void_p:
+    """C-ABI stream argument for a torch stream.  torch reports the legacy
+    default stream as handle 0, which the ABI reads as "the library's own
+    stream"; pass cudaStreamLegacy (handle 1) instead so the work is ordered
+    with the caller's."""
+    return C.c_void_p(stream.cuda_stream or 1)
+
+
 class SPHtoGridError(RuntimeError):
     """Error raised by the library; ``status`` is the ABI status code."""
 
@@ -164,6 +172,8 @@ def lib():
         L.sphg_adjoint.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
                                    C.POINTER(SphgParticles), vp, vp, C.POINTER(SphgGrads), vp]
         L.sphg_adjoint.restype = i32
+        L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]
+        L.sphg_accumulate.restype = i32
         _lib = L
     return _lib
 

@@ -79,7 +79,7 @@ class SPHMapFunction(torch.autograd.Function):
         dev = pos.device
         L = _lib.lib()
         hnd = _lib.default_context(dev.index or 0).handle
-        stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        stream = _lib.stream_handle(torch.cuda.current_stream(dev))
         pt = _particles(pos, hsml, m, rho, q, w)
         nq = pt.n_q
         P = int(param.Npixels[0])
@@ -104,7 +104,7 @@ class SPHMapFunction(torch.autograd.Function):
         dev = pos.device
         L = _lib.lib()
         hnd = _lib.default_context(dev.index or 0).handle
-        stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        stream = _lib.stream_handle(torch.cuda.current_stream(dev))
         P = int(param.Npixels[0])
         nq = 1 if q.dim() == 1 else q.shape[0]
         # dL/d(out) flattened in the output's column-major order

@@ -129,7 +129,7 @@ class SPHBatch:
     def launch(self, stream=None):
         L = _lib.lib()
         s = stream if stream is not None else torch.cuda.current_stream(self.outputs[0].device)
-        st = L.sphg_batch_launch(self.handle, C.c_void_p(s.cuda_stream))
+        st = L.sphg_batch_launch(self.handle, _lib.stream_handle(s))
         if st:
             raise _lib.SPHtoGridError(st, L.sphg_batch_last_error(self.handle).decode())
 

@@ -566,6 +566,18 @@ int sphg_reduce(sphg_context* ctx, const sphg_params* par, const sphg_options* o
   return SPHG_OK;
 }
 
+int sphg_accumulate(sphg_context* ctx, int64_t len, const double* part, double* sum, void* stream) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (len < 0 || (len > 0 && (!part || !sum))) return fail(ctx, SPHG_ERR_ARG, "NULL or negative size");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  sphg::launch_accumulate(part, sum, len, ctx->num_sms, s);
+  CK(cudaGetLastError());
+  if (!stream) CK(cudaStreamSynchronize(s));
+  return SPHG_OK;
+}
+
 int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
                  const sphg_particles* pt, const double* raw, const double* grad_out,
                  const sphg_grads* gr, void* stream) {

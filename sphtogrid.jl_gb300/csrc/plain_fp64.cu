@@ -170,6 +170,17 @@ __global__ void __launch_bounds__(256) k_reduce_3d(const double* __restrict__ q,
   }
 }
 
+// distributed_cic_map's summation of sub-file maps (distributed_mapping/cic.jl:
+// 55-78): finite entries of `part` are added into `sum`, NaN and Inf skipped.
+__global__ void __launch_bounds__(256) k_accumulate_finite(const double* __restrict__ part,
+                                                            double* __restrict__ sum, int64_t len) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < len;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = part[e];
+    if (isfinite(v)) sum[e] += v;
+  }
+}
+
 template <int DIMS>
 void launch_plain_dims(int kernel, const DevParticles& pt, const DevMapParams& mp, double* accq,
                        double* accw, int64_t PD, DevStatus* st, int grid, cudaStream_t s) {
@@ -197,6 +208,13 @@ void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& m
   if (grid > cap) grid = cap;
   if (mp.dims == 2) launch_plain_dims<2>(kernel, pt, mp, accq, accw, PD, st, (int)grid, s);
   else launch_plain_dims<3>(kernel, pt, mp, accq, accw, PD, st, (int)grid, s);
+}
+
+void launch_accumulate(const double* part, double* sum, int64_t len, int num_sms, cudaStream_t s) {
+  int64_t grid = (len + 255) / 256;
+  if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
+  if (grid < 1) grid = 1;
+  k_accumulate_finite<<<(int)grid, 256, 0, s>>>(part, sum, len);
 }
 
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s) {

@@ -195,6 +195,15 @@ __device__ __forceinline__ void axis_f(float f, float h, int a, float* dist, flo
   *ov = fminf(f + h, fa + 1.0f) - fmaxf(f - h, fa);
 }
 
+// Separable per-axis part of a cell: (squared pixel-centre offset, overlap).
+// The squared distance of a cell is (sx + sy) + sz, in that order, wherever
+// it is formed (tables or direct), so every pass sees the same u.
+__device__ __forceinline__ float2 axis_sq(float f, float h, int a) {
+  float dist, ov;
+  axis_f(f, h, a, &dist, &ov);
+  return make_float2(dist * dist, ov);
+}
+
 // Divide small non-negative integers with a float reciprocal (exact for
 // e < 2^22 and d <= 2^10 with the +0.5 guard).
 __device__ __forceinline__ int fdiv(int e, float inv_d) { return __float2int_rz(((float)e + 0.5f) * inv_d); }

@@ -164,20 +164,23 @@ __device__ inline void scan_tiles(const TiledArgs& A, long long* part) {
 // `step` starting at f0 + first, compensated (TwoSum per addition), and the
 // smallest u seen.
 template <int DIMS, int KERN>
-__device__ __forceinline__ void cell_sum_fp32(int kern, const float4 g, float h, float hinv, int a, int b, int c,
-                                              float& s, float& comp, float& umin) {
-  float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
-  axis_f(g.x, h, a, &xd, &dx);
-  axis_f(g.y, h, b, &yd, &dy);
-  if (DIMS == 3) axis_f(g.z, h, c, &zd, &dz);
-  const float u = u_of(fmaf(xd, xd, fmaf(yd, yd, zd * zd)), hinv);
+__device__ __forceinline__ void cell_term(int kern, float2 ex, float2 ey, float2 ez, float hinv, float& s,
+                                          float& comp, float& umin) {
+  const float u = u_of((ex.x + ey.x) + ez.x, hinv);
   umin = fminf(umin, u);
   if (u <= 1.0f) {
     float t, e;
-    two_sum(s, shape_f<KERN>(kern, u) * (dx * dy * dz), t, e);
+    two_sum(s, shape_f<KERN>(kern, u) * (ex.y * ey.y * ez.y), t, e);
     s = t;
     comp += e;
   }
+}
+
+template <int DIMS, int KERN>
+__device__ __forceinline__ void cell_sum_fp32(int kern, const float4 g, float h, float hinv, int a, int b, int c,
+                                              float& s, float& comp, float& umin) {
+  const float2 ez = DIMS == 3 ? axis_sq(g.z, h, c) : make_float2(0.0f, 1.0f);
+  cell_term<DIMS, KERN>(kern, axis_sq(g.x, h, a), axis_sq(g.y, h, b), ez, hinv, s, comp, umin);
 }
 
 template <int DIMS, int KERN>
@@ -204,6 +207,59 @@ __device__ __forceinline__ void record_sum_fp32(int kern, const float4 g, const 
   }
 }
 
+// Per-warp axis tables of the renormalisation pass (footprints with every
+// side at most kNormTab cells).
+constexpr int kNormTab = 64;
+
+// The whole footprint of one record from per-axis tables filled by the warp.
+template <int DIMS, int KERN>
+__device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const int4 dm, int lane, float2 (*tab)[kNormTab],
+                                               float& s, float& comp, float& umin) {
+  const float h = g.w, hinv = 1.0f / g.w;
+  const int ntab = dm.x + dm.y + (DIMS == 3 ? dm.z : 0);
+  for (int i = lane; i < ntab; i += 32) {
+    if (i < dm.x) tab[0][i] = axis_sq(g.x, h, i);
+    else if (i < dm.x + dm.y) tab[1][i - dm.x] = axis_sq(g.y, h, i - dm.x);
+    else tab[2][i - dm.x - dm.y] = axis_sq(g.z, h, i - dm.x - dm.y);
+  }
+  __syncwarp();
+  const int njk = dm.y * dm.z;
+  const int F = dm.x * njk;
+  const float inv_njk = 1.0f / (float)njk, inv_nz = 1.0f / (float)dm.z;
+  for (int f = lane; f < F; f += 32) {
+    const int a = fdiv(f, inv_njk);
+    const int rr = f - a * njk;
+    const int b = fdiv(rr, inv_nz), c = rr - b * dm.z;
+    const float2 ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
+    cell_term<DIMS, KERN>(kern, tab[0][a], tab[1][b], ez, hinv, s, comp, umin);
+  }
+  __syncwarp();  // the tables are refilled for the next record
+}
+
+// Lane 0 derives the particle's FP64 quantities (prep_particle_fp64) and
+// broadcasts the ones the cell loops need: FP64 is a small fraction of FP32
+// throughput on GB300, so the other lanes do not repeat it.
+template <int DIMS>
+__device__ __forceinline__ void prep_bcast(const DevParticles& pt, const DevMapParams& mp, int64_t p, int lane,
+                                           PrepFP64* q) {
+  PrepFP64 v;
+  v.x = v.y = v.z = v.hsml = v.h_inv = v.knorm = v.area = v.col = v.vol = v.m_in = v.rho_in = v.wgt = 0.0;
+  if (lane == 0) prep_particle_fp64<DIMS>(pt, mp, p, false, &v);
+  const unsigned full = 0xffffffffu;
+  q->x = __shfl_sync(full, v.x, 0);
+  q->y = __shfl_sync(full, v.y, 0);
+  q->z = __shfl_sync(full, v.z, 0);
+  q->hsml = __shfl_sync(full, v.hsml, 0);
+  q->h_inv = __shfl_sync(full, v.h_inv, 0);
+  q->knorm = __shfl_sync(full, v.knorm, 0);
+  q->area = v.area;  // lane 0 only: the per-particle factors
+  q->col = v.col;
+  q->vol = v.vol;
+  q->m_in = v.m_in;
+  q->rho_in = v.rho_in;
+  q->wgt = v.wgt;
+}
+
 // Compensated butterfly reduction of (s, comp) and min of umin over a warp.
 __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& umin) {
 #pragma unroll
@@ -223,8 +279,8 @@ __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& u
 // particles), channel exponents, deterministic bounds, mass diagnostic and the
 // record's entries in the tile lists.
 template <int DIMS, int KERN>
-__device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umin, int lane, bool overflow,
-                              double& c_gm, int* emax, unsigned long long* bacc) {
+__device__ void finish_record(const TiledArgs& A, int64_t r, float S, float S_err, float umin, int lane,
+                              bool overflow, double& c_gm, int* emax, unsigned long long* bacc) {
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
   const int njk = dm.y * dm.z;
@@ -244,11 +300,11 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
   int fl = 0;
   double bound = 0.0;  // largest per-cell weight of this particle
   double gm = 0.0;
-  if (umin > 0.9f || !(S > 0.0)) {
+  if (umin > 0.9f || !(S > 0.0f)) {
     // ill-conditioned (every pixel centre near or beyond the kernel edge):
     // the reference's FP64 arithmetic, as in the plain path
     PrepFP64 q;
-    prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+    prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
     double s_w = 0.0, s_a = 0.0;
     long long n_d = 0, n_t = 0;
     for (int64_t f = lane; f < F; f += 32) {
@@ -269,22 +325,25 @@ __device__ void finish_record(const TiledArgs& A, int64_t r, double S, float umi
     n_d = warp_sum_ll(n_d);
     n_t = warp_sum_ll(n_t);
     const bool fallback = (s_w == 0.0);
-    double wpp;
-    if (fallback) {
-      n_d = n_t;
-      wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
-    } else {
-      wpp = (double)n_d / s_w;
-    }
-    cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
-                    : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
     fl = kRecFP64 | (fallback ? kRecFallback : 0);
-    bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
-    gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    if (lane == 0) {  // per-particle factors (the scalars of prep_bcast live on lane 0)
+      double wpp;
+      if (fallback) {
+        n_d = n_t;
+        wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
+      } else {
+        wpp = (double)n_d / s_w;
+      }
+      cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                      : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
+      bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
+      gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    }
   } else if (lane == 0) {  // FP64 on one lane: GB300's FP64 rate is a small fraction of FP32
-    cpv = A.cp[r] / S;
+    const double Sd = (double)S + (double)S_err;
+    cpv = A.cp[r] / Sd;
     bound = fabs(cpv);
-    gm = A.aux[r] * S;
+    gm = A.aux[r] * Sd;
   }
   if (lane == 0) {
     A.cp[r] = cpv;
@@ -346,14 +405,19 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
     emax[c] = INT_MIN;
     bacc[c] = 0ull;
   }
+  __shared__ float2 tabs[8][3][kNormTab];  // one set per warp of a 256-thread CTA
+  float2(*tab)[kNormTab] = tabs[(threadIdx.x >> 5) & 7];
   for (int64_t r = wid; r < nrec; r += nw) {
     const int4 dm = A.dimv[r];
     const int64_t F = (int64_t)dm.x * dm.y * dm.z;
     if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
     float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-    record_sum_fp32<DIMS, KERN>(A.kern, A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
+    if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab)
+      record_sum_tab<DIMS, KERN>(A.kern, A.geo[r], dm, lane, tab, s, comp, umin);
+    else
+      record_sum_fp32<DIMS, KERN>(A.kern, A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
     warp_reduce_comp(s, comp, umin);
-    finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax, bacc);
+    finish_record<DIMS, KERN>(A, r, s, comp, umin, lane, overflow, c_gm, emax, bacc);
   }
   flush_stats(A, lane, DIMS, c_gm, emax, bacc);
 }
@@ -443,7 +507,7 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
         umin = fminf(umin, pv.z);
       }
       warp_reduce_comp(s, comp, umin);
-      finish_record<DIMS, KERN>(A, r, (double)s + (double)comp, umin, lane, overflow, c_gm, emax, bacc);
+      finish_record<DIMS, KERN>(A, r, s, comp, umin, lane, overflow, c_gm, emax, bacc);
     }
   }
   flush_stats(A, lane, DIMS, c_gm, emax, bacc);
@@ -508,6 +572,9 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
   const double scw = s_scale[nq];
+  // per-warp axis tables of the current pair's intersection with the tile
+  __shared__ float2 dtabs[8][3][32];
+  float2(*tab)[32] = dtabs[warp & 7];
   for (long long s = p0 + warp; s < p1; s += nwarp) {
     const int r = A.pairs[s];
     const int4 bx = A.box[r];
@@ -518,19 +585,13 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
     const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
     const int n = na * nb * nc;
-    // per-record factors in FP32: cp = cpm * 2^cpe, shifted by the channel scale
-    const float cpm = A.cpm[r];
-    const int cpe = A.cpe[r];
-    const float cw = ldexpf(cpm, cpe + s_shift[nq]);
-    float cq[NQ > 0 ? NQ : kMaxQ];
-    for (int k = 0; k < nq; ++k) cq[k] = ldexpf(cpm * A.qv[(int64_t)k * A.cap + r], cpe + s_shift[k]);
     const float inv_nc = 1.0f / (float)nc, inv_nb = 1.0f / (float)nb;
     // local-frame offset of the tile origin
     const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
     if (bx.w & kRecFP64) {
       // ill-conditioned particle: per-cell weights in the reference's FP64
       PrepFP64 q;
-      prep_particle_fp64<DIMS>(A.pt, A.mp_re, dm.w, false, &q);
+      prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
       const bool fb = (bx.w & kRecFallback) != 0;
       const double cpv = A.cp[r];
       for (int e = lane; e < n; e += 32) {
@@ -553,23 +614,32 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       }
       continue;
     }
+    // per-record factors in FP32: cp = cpm * 2^cpe, shifted by the channel scale
+    const float cpm = A.cpm[r];
+    const int cpe = A.cpe[r];
+    const float cw = ldexpf(cpm, cpe + s_shift[nq]);
+    float cq[NQ > 0 ? NQ : kMaxQ];
+    for (int k = 0; k < nq; ++k) cq[k] = ldexpf(cpm * A.qv[(int64_t)k * A.cap + r], cpe + s_shift[k]);
     const float4 g = A.geo[r];
     const float h = g.w, hinv = 1.0f / g.w;
+    for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms
+      if (i < na) tab[0][i] = axis_sq(g.x, h, a0 + i);
+      else if (i < na + nb) tab[1][i - na] = axis_sq(g.y, h, b0 + i - na);
+      else tab[2][i - na - nb] = DIMS == 3 ? axis_sq(g.z, h, c0 + i - na - nb) : make_float2(0.0f, 1.0f);
+    }
+    __syncwarp();
+    const int lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
     for (int e = lane; e < n; e += 32) {
       const int bc = fdiv(e, inv_nc);
       const int c = e - bc * nc;
       const int a = fdiv(bc, inv_nb);
       const int b = bc - a * nb;
-      const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
-      float xd, dx, yd, dy, zd = 0.0f, dz = 1.0f;
-      axis_f(g.x, h, ia, &xd, &dx);
-      axis_f(g.y, h, jb, &yd, &dy);
-      if (DIMS == 3) axis_f(g.z, h, kc, &zd, &dz);
-      const float u = u_of(fmaf(xd, xd, fmaf(yd, yd, zd * zd)), hinv);
+      const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
+      const float u = u_of((ex.x + ey.x) + ez.x, hinv);
       if (u <= 1.0f) {
-        const float gw = shape_f<KERN>(A.kern, u) * (dx * dy * dz);
+        const float gw = shape_f<KERN>(A.kern, u) * (ex.y * ey.y * ez.y);
         if (gw != 0.0f) {
-          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+          const int li = lbase + (a * TY + b) * TZ + c;
           acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
           for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
@@ -579,6 +649,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
         }
       }
     }
+    __syncwarp();  // the tables are refilled for the next pair
   }
   __syncthreads();
   // flush: FP64 values straight into the output layout
@@ -622,7 +693,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-__global__ void __launch_bounds__(256) k_deposit(TiledArgs A) {
+__global__ void __launch_bounds__(256, 4) k_deposit(TiledArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw);
 }

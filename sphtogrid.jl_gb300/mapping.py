@@ -88,7 +88,7 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
                reduce_image: bool = True, return_both_maps: bool = False, dimensions: int = 2,
                calc_mean: bool = False, stokes: bool = False, sort_z: bool = False,
                precision: str = "fp64", deterministic: bool = False, device: int = 0,
-               return_stats: bool = False):
+               return_stats: bool = False, center_in_place: bool = True):
     """Map particle quantities to a 2D projected or 3D gridded image.
 
     Arguments and keywords are those of the reference; ``parallel`` is
@@ -96,7 +96,8 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     ``precision`` ("fp64": the reference's arithmetic; "fp32c": FP32 weights
     with compensated sums), ``deterministic`` (bitwise reproducible sums),
     ``device`` (host inputs: which GPU), ``return_stats`` (also return a dict
-    with particle / deposit counts and the 3D mass diagnostic).
+    with particle / deposit counts and the 3D mass diagnostic),
+    ``center_in_place`` (False: centre on the fly and leave ``Pos`` as it is).
     """
     if RM is not None or stokes:
         raise NotImplementedError(
@@ -112,11 +113,12 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     on_device = _is_torch_cuda(Pos)
     if on_device:
         out = _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image,
-                         return_both_maps, dimensions, calc_mean, sort_z, precision, deterministic)
+                         return_both_maps, dimensions, calc_mean, sort_z, precision, deterministic,
+                         center_in_place)
     else:
         out = _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image,
                          return_both_maps, dimensions, calc_mean, sort_z, precision, deterministic,
-                         device)
+                         device, center_in_place)
     image, stats = out
     if show_progress:
         log.info("sphMapping: %d / %d particles mapped, %d deposits, %.3f s",
@@ -124,7 +126,7 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     return (image, stats) if return_stats else image
 
 def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
-               dims, calc_mean, sort_z, precision, deterministic, device):
+               dims, calc_mean, sort_z, precision, deterministic, device, center_in_place=True):
     if not isinstance(Pos, np.ndarray) or Pos.ndim != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) array")
     n = Pos.shape[1]
@@ -153,7 +155,8 @@ def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
             raise ValueError("particle arrays must have N entries")
     if q.shape[-1] != n:
         raise ValueError("Bin_Quant must have N columns")
-    center_mode, filt = _lib.CENTER_INPLACE, 1
+    center_mode = _lib.CENTER_INPLACE if center_in_place else _lib.CENTER_READONLY
+    filt = 1
     if sort_z:
         # filter_shift.jl:61-63: z-sorted (descending) index list, selected by
         # the mask in input order -- the reference's selection, kept as is.
@@ -217,7 +220,7 @@ def _torch_dt(t):
     raise TypeError(f"unsupported dtype {t.dtype}")
 
 def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
-               dims, calc_mean, sort_z, precision, deterministic):
+               dims, calc_mean, sort_z, precision, deterministic, center_in_place=True):
     import torch
     if Pos.dim() != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) tensor")
@@ -237,7 +240,8 @@ def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
         raise ValueError("Pos strides must be non-negative")
     P = int(param.Npixels[0])
     opts = _options(param, kernel, dims, reduce_image, return_both_maps, calc_mean, precision,
-                    deterministic, _lib.CENTER_INPLACE, 1, _lib.MEM_DEVICE)
+                    deterministic, _lib.CENTER_INPLACE if center_in_place else _lib.CENTER_READONLY,
+                    1, _lib.MEM_DEVICE)
     out_len = _lib.lib().sphg_output_len(C.byref(param._c), C.byref(opts), nq)
     flat = torch.empty(out_len, dtype=torch.float64, device=dev)
     pt = _lib.SphgParticles()
@@ -255,8 +259,8 @@ def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
         pt.q_stride_p, pt.q_stride_k = q.stride(1), q.stride(0)
     st = _lib.SphgStats()
     ctx = _lib.default_context(dev.index if dev.index is not None else 0)
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    stream = _lib.stream_handle(torch.cuda.current_stream(dev))
     _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
-                                   C.c_void_p(flat.data_ptr()), C.c_void_p(stream), C.byref(st)),
+                                   C.c_void_p(flat.data_ptr()), stream, C.byref(st)),
                ctx.handle)
     return _shape_out(flat, P, nq, dims, return_both_maps and dims == 2), _stats_dict(st)
