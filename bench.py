@@ -196,6 +196,13 @@ def bench_gpu(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.batched_only:  # profiling runs: the batched workload alone
+        import __graft_entry__ as graft
+        b = bench_batched(graft.load_package(), dev, args.steps, args.warmup)
+        if rank == 0:
+            b.pop("rel_err_per_map")
+            print(json.dumps(b), flush=True)
+        return 0
     pkg, d = load_workload()
     from sphtogrid_gb300 import _lib
     L = _lib.lib()
@@ -204,7 +211,7 @@ def bench_gpu(args):
     P = d["npix"]
     par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
 
-    def opts(prec, mem, profile=1):
+    def opts(prec, mem, profile=1, det=None):
         o = _lib.SphgOptions()
         o.dimensions = 3
         o.kernel = pkg.WendlandC6(3).kind
@@ -215,7 +222,7 @@ def bench_gpu(args):
         o.filter = 1
         o.memspace = mem
         o.profile = profile
-        o.deterministic = int(args.deterministic and prec == "fp32c")
+        o.deterministic = int((args.deterministic if det is None else det) and prec == "fp32c")
         return o
 
     # device-resident inputs (Julia layout: xyz contiguous per particle)
@@ -229,16 +236,16 @@ def bench_gpu(args):
     stream = torch.cuda.current_stream(dev)
     sh = _lib.stream_handle(stream)  # the events below bracket work on this stream
 
-    def step(prec, st, pt=pt_dev, out=None, mem=_lib.MEM_DEVICE, profile=1):
-        o = opts(prec, mem, profile)
+    def step(prec, st, pt=pt_dev, out=None, mem=_lib.MEM_DEVICE, profile=1, det=None):
+        o = opts(prec, mem, profile, det)
         dst = C.c_void_p(t_out.data_ptr()) if out is None else out
         _lib.check(L.sphg_map(ctx.handle, C.byref(par._c), C.byref(o), C.byref(pt), dst, sh,
                               C.byref(st)), ctx.handle)
 
-    def timed(prec, steps, warmup):
+    def timed(prec, steps, warmup, det=None):
         st = _lib.SphgStats()
         for _ in range(warmup):
-            step(prec, st)
+            step(prec, st, det=det)
         torch.cuda.synchronize(dev)
         if dist is not None:
             dist.barrier()
@@ -248,7 +255,7 @@ def bench_gpu(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            step(prec, st)
+            step(prec, st, det=det)
             phases += np.array(list(st.phase_ms))
             launches += st.n_launches
         e1.record(stream)
@@ -284,6 +291,20 @@ def bench_gpu(args):
     torch.cuda.synchronize(dev)
     img_main = t_out.clone()
     rel_vs_fp64 = _rel_linf(img_main.cpu().numpy(), img_fp64.cpu().numpy())
+    other = None  # the other accumulation mode of the FP32C method, same map
+    if prec == "fp32c":
+        det2 = not args.deterministic
+        ms2, _, ph2, _ = timed(prec, args.steps, args.warmup, det=det2)
+        step(prec, _lib.SphgStats(), det=det2)
+        torch.cuda.synchronize(dev)
+        other = {"deterministic": det2, "ms_per_step": ms2 / args.steps,
+                 "value": deposits * args.steps / (ms2 * 1e-3),
+                 "phases_ms": {"prep": float(ph2[0]), "norm": float(ph2[1]),
+                               "deposit": float(ph2[2]), "reduce": float(ph2[3])},
+                 "rel_linf_vs_fp64": _rel_linf(t_out.cpu().numpy(), img_fp64.cpu().numpy())}
+    batched = None
+    if rank == 0 and world == 1 and not args.no_batched:
+        batched = bench_batched(pkg, dev, args.steps, args.warmup)
 
     # end to end through the C ABI with pinned host buffers
     h_pos = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).pin_memory()
@@ -338,6 +359,10 @@ def bench_gpu(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if other is not None:
+        line["fp32c_other_mode"] = other
+    if batched is not None:
+        line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         O = oracle_module()
         dt, dep, img_ref, threads, m = run_oracle(O, d, frac=args.cpu_frac)
@@ -353,6 +378,90 @@ def bench_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e6], Npixels in "
+                  "{128, 256, 512, 1024}, 1-4 quantities (rho, lognormal temperature, Gaussian "
+                  "velocity component sigma 300, lognormal |B|), Quintic and WendlandC4 mixed, "
+                  "Float32, seed 0; one persistent work-queue launch per phase, CUDA graph replay, "
+                  "autotuned tiles")
+
+
+def bench_batched(pkg, dev, steps, warmup):
+    """The batched uneven-maps workload: maps/s of one graph-replayed batch
+    against the plain FP64 method called map by map, and each map's error
+    against the plain FP64 map (on pixels with W >= 1e-6 max W, relative to
+    the map of |q| where quantities of both signs cancel)."""
+    import torch
+    from sphtogrid_gb300 import synth
+    from sphtogrid_gb300.batch import MapSpec, SPHBatch
+    maps = synth.batched_2d()
+    specs, host = [], []
+    for d in maps:
+        par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["npix"])
+        tp = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).to(dev).T
+        ts = [torch.from_numpy(np.ascontiguousarray(d[k])).to(dev)
+              for k in ("hsml", "mass", "rho", "bin_q", "weights")]
+        kern = pkg.kernel_from_name(d["kernel"], 2)
+        specs.append(MapSpec(tp, *ts, param=par, kernel=kern, dimensions=2))
+        host.append((par, tp, ts, kern))
+    t0 = time.perf_counter()
+    b = SPHBatch(specs)  # plans, autotunes and captures the graph
+    plan_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        b.launch()
+    stats = b.wait()
+    deposits = sum(x["deposits"] for x in stats)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        b.launch()
+    e1.record(stream)
+    b.wait()
+    ms_batch = e0.elapsed_time(e1) / steps
+
+    def one(par, tp, ts, kern, q=None, raw=False):
+        h, m, rho, bq, w = ts
+        return pkg.sphMapping(tp, h, m, rho, bq if q is None else q, w, param=par, kernel=kern,
+                              precision="fp64", return_both_maps=raw, show_progress=False,
+                              center_in_place=False)
+
+    for x in host[:4]:
+        one(*x)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for x in host:
+        one(*x)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms64 = e0.elapsed_time(e1)
+    errs = []
+    for i, x in enumerate(host):
+        par = x[0]
+        P = int(par.Npixels[0])
+        raw = one(*x, raw=True).cpu().numpy()
+        absq = one(*x, q=x[2][3].abs(), raw=True).cpu().numpy()
+        W = raw[:, -1:]
+        nq = raw.shape[1] - 1
+        ref = np.where(W > 0, raw[:, :nq] / np.where(W > 0, W, 1.0), raw[:, :nq])
+        scale = np.where(W > 0, absq[:, :nq] / np.where(W > 0, W, 1.0), absq[:, :nq])
+        got = b.image(i).cpu().numpy().reshape(P * P, nq)  # [x, y, q] -> rows x*P + y
+        keep = np.repeat(W >= 1e-6 * W.max(), nq, axis=1)
+        den = np.maximum(np.abs(ref), scale)
+        sel = keep & (den > 0)
+        errs.append(float((np.abs(got - ref)[sel] / den[sel]).max()) if sel.any() else 0.0)
+    n = len(maps)
+    out = {"workload": BATCH_WORKLOAD, "maps": n,
+           "particles": int(sum(d["pos"].shape[1] for d in maps)),
+           "deposits_per_batch": int(deposits), "ms_per_batch": ms_batch,
+           "maps_per_s": 1e3 * n / ms_batch, "deposits_per_s": deposits / (ms_batch * 1e-3),
+           "plain_fp64_maps_per_s": 1e3 * n / ms64, "speedup_vs_plain_fp64": ms64 / ms_batch,
+           "rel_err_max": max(errs), "rel_err_median": float(np.median(errs)),
+           "rel_err_per_map": [float(f"{e:.3g}") for e in errs],
+           "tuning": b.tuning, "plan_and_autotune_s": plan_s}
+    b.close()
+    return out
 
 
 def _rel_linf(a, b, floor=1e-9):
@@ -401,6 +510,10 @@ def main():
                     help="bitwise reproducible int64 fixed-point tile sums")
     ap.add_argument("--only-device", action="store_true",
                     help="time the device-resident loop only (for profiler runs)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched 96-map workload")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="time the batched 96-map workload alone (for profiler runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

@@ -360,7 +360,7 @@ again:
     o_start = cv.take((ta.n_tiles + 1) * sizeof(long long));
     o_pairs = cv.take(pair_cap * sizeof(int));
     o_nrec = o_cnt + 2 * ta.n_tiles * sizeof(int);
-    o_exps = cv.take(2 * (sphg::kMaxQ + 1) * sizeof(int) + (sphg::kMaxQ + 1) * sizeof(unsigned long long));
+    o_exps = cv.take((sphg::kMaxQ + 1) * sizeof(int));
     o_large = cv.take(cap * sizeof(int));
     o_lstart = cv.take((cap + 1) * sizeof(long long));
     o_part = cv.take(chunk_cap * sizeof(float4));
@@ -481,8 +481,6 @@ again:
     ta.pairs = (int*)(ws + o_pairs);
     ta.pair_cap = pair_cap;
     ta.exps = (int*)(ws + o_exps);
-    ta.kexp = ta.exps + (sphg::kMaxQ + 1);
-    ta.bsum = (unsigned long long*)(ta.kexp + (sphg::kMaxQ + 1));
     ta.det = opt->deterministic ? 1 : 0;
     ta.n_large = ta.n_rec + 1;
     ta.large = (int*)(ws + o_large);
@@ -498,8 +496,7 @@ again:
     ta.reduce = opt->reduce_image;
     ta.w_is_one = opt->reduce_image ? 0 : 1;
     CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 2) * sizeof(int), s));
-    CK(cudaMemsetAsync(ta.exps, 0x80, 2 * (sphg::kMaxQ + 1) * sizeof(int), s));
-    CK(cudaMemsetAsync(ta.bsum, 0, (sphg::kMaxQ + 1) * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ta.exps, 0x80, (sphg::kMaxQ + 1) * sizeof(int), s));
     CK(sphg::launch_tiled_fp32(opt->kernel, ta, ctx->num_sms, s, ev, &n_launch));
     if (ev) CK(cudaEventRecord(ev[4], s));
   }

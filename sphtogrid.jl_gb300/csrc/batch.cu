@@ -165,8 +165,7 @@ struct BatchPlan {
   DevStatus* d_status = nullptr;  // per map
   char* counters = nullptr;
   size_t counters_bytes = 0;
-  int* exps = nullptr;            // per map 2 x (kMaxQ + 1)
-  unsigned long long* bsum = nullptr;  // per map kMaxQ + 1
+  int* exps = nullptr;            // per map kMaxQ + 1
   size_t smem = 0;
   bool det = false;
   int k1_grid = 0;
@@ -237,8 +236,7 @@ int build_plan(sphg_batch* b) {
     cnt_bytes += (2 * b->maps[m].n_tiles + 2) * sizeof(int);
   }
   const size_t o_cnt = take(cnt_bytes);
-  const size_t o_exps = take((size_t)nm * 2 * (kMaxQ + 1) * sizeof(int));
-  const size_t o_bsum = take((size_t)nm * (kMaxQ + 1) * sizeof(unsigned long long));
+  const size_t o_exps = take((size_t)nm * (kMaxQ + 1) * sizeof(int));
   const size_t o_stat = take((size_t)nm * sizeof(DevStatus) + sizeof(unsigned long long));
   const size_t o_args = take((size_t)nm * sizeof(TiledArgs));
   const size_t o_meta = take((size_t)(nm + 1) * sizeof(int) + (size_t)(nm + 1) * sizeof(long long) +
@@ -276,7 +274,6 @@ int build_plan(sphg_batch* b) {
   p.counters = base + o_cnt;
   p.counters_bytes = cnt_bytes;
   p.exps = (int*)(base + o_exps);
-  p.bsum = (unsigned long long*)(base + o_bsum);
   p.d_status = (DevStatus*)(base + o_stat);
   p.d_args = (TiledArgs*)(base + o_args);
   p.smem = smem;
@@ -365,9 +362,7 @@ int build_plan(sphg_batch* b) {
     A.large_start = (long long*)(base + o.lstart);
     A.partials = (float4*)(base + o.part);
     A.chunk_cap = M.chunk_cap;
-    A.exps = p.exps + (size_t)m * 2 * (kMaxQ + 1);
-    A.kexp = A.exps + (kMaxQ + 1);
-    A.bsum = p.bsum + (size_t)m * (kMaxQ + 1);
+    A.exps = p.exps + (size_t)m * (kMaxQ + 1);
     A.det = p.det ? 1 : 0;
     A.st = p.d_status + m;
     A.out = D.out;
@@ -403,8 +398,7 @@ int enqueue(sphg_batch* b, cudaStream_t s) {
   BatchPlan& p = b->plan;
   const int nm = (int)b->maps.size();
   BCK(cudaMemsetAsync(p.counters, 0, p.counters_bytes, s));
-  BCK(cudaMemsetAsync(p.exps, 0x80, (size_t)nm * 2 * (kMaxQ + 1) * sizeof(int), s));
-  BCK(cudaMemsetAsync(p.bsum, 0, (size_t)nm * (kMaxQ + 1) * sizeof(unsigned long long), s));
+  BCK(cudaMemsetAsync(p.exps, 0x80, (size_t)nm * (kMaxQ + 1) * sizeof(int), s));
   BCK(cudaMemsetAsync(p.d_status, 0, (size_t)nm * sizeof(DevStatus) + sizeof(unsigned long long), s));
   kb_prep<<<p.k1_grid, 256, 0, s>>>(p.dev);
   kb_scan<<<nm, 1024, 0, s>>>(p.dev);

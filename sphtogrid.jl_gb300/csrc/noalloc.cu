@@ -142,7 +142,7 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   const size_t o_aux = take(cap * sizeof(double)), o_qv = take(cap * nq * sizeof(float));
   const size_t o_cnt = take((2 * ta.n_tiles + 2) * sizeof(int));
   const size_t o_start = take((ta.n_tiles + 1) * sizeof(long long));
-  const size_t o_exps = take(2 * (kMaxQ + 1) * sizeof(int) + (kMaxQ + 1) * sizeof(unsigned long long));
+  const size_t o_exps = take((kMaxQ + 1) * sizeof(int));
   const size_t o_large = take(cap * sizeof(int)), o_lstart = take((cap + 1) * sizeof(long long));
   if (off + al(4096 * sizeof(float4)) + al((size_t)ta.n_tiles * sizeof(int)) > kNoAllocScratchBytes)
     return nfail(SPHG_ERR_ARG, std::to_string(n) + " particles on a " + std::to_string(P) + "^" +
@@ -222,8 +222,6 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   ta.pairs = (int*)(ws + o_pairs);
   ta.pair_cap = (long long)(pair_bytes / sizeof(int));
   ta.exps = (int*)(ws + o_exps);
-  ta.kexp = ta.exps + (kMaxQ + 1);
-  ta.bsum = (unsigned long long*)(ta.kexp + (kMaxQ + 1));
   ta.det = opt->deterministic ? 1 : 0;
   ta.large = (int*)(ws + o_large);
   ta.large_start = (long long*)(ws + o_lstart);
@@ -241,8 +239,7 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   // call's contents)
   cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(DevStatus), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 2) * sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ta.exps, 0x80, 2 * (kMaxQ + 1) * sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ta.bsum, 0, (kMaxQ + 1) * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ta.exps, 0x80, (kMaxQ + 1) * sizeof(int), s);
   if (e == cudaSuccess) e = launch_tiled_fp32(opt->kernel, ta, slot.num_sms, s, nullptr, nullptr);
   DevStatus hs;
   std::memset(&hs, 0, sizeof(hs));

@@ -57,7 +57,8 @@ struct TiledArgs {
   double* cp;       // K1: numerator of the weight factor; K3: the factor
   float* cpm;       // K3: the factor as FP32 mantissa ...
   int* cpe;         //     ... and binary exponent (cp = cpm * 2^cpe)
-  double* aux;      // rho / L^3 * kernel normalisation (3D mass diagnostic)
+  double* aux;      // K1: rho / L^3 * kernel normalisation (3D mass diagnostic);
+                    // K3: |numerator|, the record's total deposit into W
   float* qv;        // quantities, qv[k * cap + r]
   int* tile_count;  // per tile, zeroed before K1
   int* tile_fill;   // per tile, zeroed before K3
@@ -72,10 +73,8 @@ struct TiledArgs {
   long long chunk_cap;
   int large_grid;
   int* exps;        // per channel max exponent (channels 0..nq-1 = Q, nq = W)
-  // deterministic mode: exact int64 fixed-point tile sums
+  // deterministic mode: exact int64 fixed-point tile sums, scaled per tile
   int det;
-  int* kexp;                  // K1: per channel max exponent of a particle's total
-  unsigned long long* bsum;   // K3: per channel integer bound of the channel total
   DevStatus* st;
   // output
   double* out;
@@ -118,17 +117,6 @@ __device__ __forceinline__ void acc_twosum(float* hi, float* lo, float v) {
   if (e != 0.0f) atomicAdd(lo, e);
 }
 
-// Fixed-point scale exponent of a channel in the deterministic mode: every
-// partial sum of the channel stays below 2^62 in magnitude.  The bound is the
-// integer sum (bsum + one unit per record) of per-particle totals in units of
-// 2^(kexp - 30), widened by 2^-20 for the FP32 rounding of the cell values.
-__device__ __forceinline__ int fixed_exponent(int kexp, unsigned long long bsum, int nrec) {
-  if (kexp < -100000 || bsum == 0ull) return 0;
-  const double bound = ldexp((double)bsum + (double)nrec + 1.0, kexp - 30) * (1.0 + 0x1p-20);
-  int e;
-  frexp(bound, &e);  // bound < 2^e
-  return 62 - e;
-}
 
 // FP32 kernel shape (no normalisation) via fused multiply-adds.
 template <int KERN>
@@ -204,8 +192,32 @@ __device__ __forceinline__ float2 axis_sq(float f, float h, int a) {
   return make_float2(dist * dist, ov);
 }
 
-// Divide small non-negative integers with a float reciprocal (exact for
-// e < 2^22 and d <= 2^10 with the +0.5 guard).
+// q = m * 2^e with m in [0.5, 1) for normal floats, by bit operations (no
+// branches); zero, subnormal and non-finite q are returned as m = q, e = 0.
+__device__ __forceinline__ void split_f(float q, float& m, int& e) {
+  const unsigned b = __float_as_uint(q);
+  const int be = (int)((b >> 23) & 0xffu);
+  const bool normal = be != 0 && be != 255;
+  m = normal ? __uint_as_float((b & 0x807fffffu) | (126u << 23)) : q;
+  e = normal ? be - 126 : 0;
+}
+
+// Divide small non-negative integers with a float reciprocal: with inv_d
+// within 2^-21 (relative) of 1/d, trunc((e + 0.5) * inv_d) == e / d for
+// 0 <= e < 2^20, since (e + 0.5) / d stays at least 0.5 / d away from an
+// integer and the error of the product is below (e + 0.5) * 2^-20 / d.
 __device__ __forceinline__ int fdiv(int e, float inv_d) { return __float2int_rz(((float)e + 0.5f) * inv_d); }
+
+// Reciprocal of a positive integer for fdiv: the approximate reciprocal
+// (within 2 ulp), one instruction instead of the correctly rounded division.
+__device__ __forceinline__ float inv_small(int d) { return __fdividef(1.0f, (float)d); }
+
+// 2^k as a float for -126 <= k <= 127, 0 below (the values scaled by it are
+// then below 2^-126 of the channel's largest and do not change the sums),
+// infinity above; exact, without the special-case branches of ldexpf.
+__device__ __forceinline__ float pow2f(int k) {
+  const int kc = k < -127 ? -127 : (k > 128 ? 128 : k);
+  return __int_as_float((kc + 127) << 23);
+}
 
 }  // namespace sphg

@@ -22,9 +22,6 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
   unsigned long long c_mapped = 0, c_dep = 0;
   double c_pm = 0.0;
   unsigned flags = 0;
-  int kmax[kMaxQ + 1];
-  if (A.det)
-    for (int c = 0; c <= A.pt.nq; ++c) kmax[c] = INT_MIN;
   for (int64_t base = base0; base < A.pt.n; base += stride) {
     const int64_t p = base + threadIdx.x;
     PrepFP64 q;
@@ -63,21 +60,6 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
       for (int k = 0; k < A.pt.nq; ++k)
         A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
             : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
-      if (A.det) {  // exponent of the particle's total per channel
-        const double num = fabs(A.cp[r]);
-        int e;
-        if (num > 0.0 && num < 1e300) {
-          frexp(num, &e);
-          kmax[A.pt.nq] = max(kmax[A.pt.nq], e);
-          for (int k = 0; k < A.pt.nq; ++k) {
-            const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
-            if (qa > 0.0 && qa < 1e300) {
-              frexp(num * qa, &e);
-              kmax[k] = max(kmax[k], e);
-            }
-          }
-        }
-      }
       if ((int64_t)ni * nj * nk > A.large_cells) A.large[atomicAdd(A.n_large, 1)] = r;
       // (particle, tile) overlaps
       const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
@@ -93,11 +75,6 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
   c_mapped = (unsigned long long)warp_sum_ll((long long)c_mapped);
   c_dep = (unsigned long long)warp_sum_ll((long long)c_dep);
   flags = __reduce_or_sync(0xffffffffu, flags);
-  if (A.det)  // one atomic per warp and channel
-    for (int c = 0; c <= A.pt.nq; ++c) {
-      const int km = __reduce_max_sync(0xffffffffu, kmax[c]);
-      if (lane == 0 && km != INT_MIN) atomicMax(&A.kexp[c], km);
-    }
   if (lane == 0) {
     if (c_mapped) {
       atomicAdd(&A.st->n_mapped, c_mapped);
@@ -188,9 +165,9 @@ __device__ __forceinline__ void record_sum_fp32(int kern, const float4 g, const 
                                                 int first, int step, float& s, float& comp, float& umin) {
   const int njk = dm.y * dm.z;
   const float h = g.w, hinv = 1.0f / g.w;
-  if (f1 + njk < (1 << 21)) {
+  if (f1 + njk < (1 << 20)) {
     // 32-bit cell index, decomposed with float reciprocals (exact here)
-    const float inv_njk = 1.0f / (float)njk, inv_nz = 1.0f / (float)dm.z;
+    const float inv_njk = inv_small(njk), inv_nz = inv_small(dm.z);
     for (int f = (int)f0 + first; f < (int)f1; f += step) {
       const int a = fdiv(f, inv_njk);
       const int rr = f - a * njk;
@@ -217,15 +194,15 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
                                                float& s, float& comp, float& umin) {
   const float h = g.w, hinv = 1.0f / g.w;
   const int ntab = dm.x + dm.y + (DIMS == 3 ? dm.z : 0);
-  for (int i = lane; i < ntab; i += 32) {
-    if (i < dm.x) tab[0][i] = axis_sq(g.x, h, i);
-    else if (i < dm.x + dm.y) tab[1][i - dm.x] = axis_sq(g.y, h, i - dm.x);
-    else tab[2][i - dm.x - dm.y] = axis_sq(g.z, h, i - dm.x - dm.y);
+  for (int i = lane; i < ntab; i += 32) {  // axis and offset by selects (no divergence)
+    const int ax = i < dm.x ? 0 : (i < dm.x + dm.y ? 1 : 2);
+    const int k = i - (ax == 0 ? 0 : (ax == 1 ? dm.x : dm.x + dm.y));
+    tab[ax][k] = axis_sq(ax == 0 ? g.x : (ax == 1 ? g.y : g.z), h, k);
   }
   __syncwarp();
   const int njk = dm.y * dm.z;
   const int F = dm.x * njk;
-  const float inv_njk = 1.0f / (float)njk, inv_nz = 1.0f / (float)dm.z;
+  const float inv_njk = inv_small(njk), inv_nz = inv_small(dm.z);
   for (int f = lane; f < F; f += 32) {
     const int a = fdiv(f, inv_njk);
     const int rr = f - a * njk;
@@ -274,155 +251,188 @@ __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& u
   }
 }
 
-// Finishes one record with the whole warp, given its FP32 renormalisation sum
-// S and smallest u: weight factor (or the FP64 redo of ill-conditioned
-// particles), channel exponents, deterministic bounds, mass diagnostic and the
-// record's entries in the tile lists.
+// Stores the finished weight factor cpv of record r (FP64, and as FP32
+// mantissa and exponent for the deposit) in place of its numerator, and
+// raises the channel exponents by the record's largest per-cell weight
+// `bound`.
+__device__ __forceinline__ void store_factor(const TiledArgs& A, int64_t r, double cpv, double bound, int fl,
+                                             int* emax) {
+  // Dolag renormalisation makes the record's deposits into W sum to the
+  // numerator; the deterministic mode bounds its tile sums with it
+  A.aux[r] = fabs(A.cp[r]);
+  A.cp[r] = cpv;
+  int ce = 0;
+  const float cm = (float)frexp(cpv, &ce);
+  A.cpm[r] = cm;
+  A.cpe[r] = ce;
+  if (fl) A.box[r].w = fl;
+  int e;
+  if (bound > 0.0 && bound < 1e300) {
+    frexp(bound, &e);
+    emax[A.pt.nq] = max(emax[A.pt.nq], e);
+    for (int k = 0; k < A.pt.nq; ++k) {
+      const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
+      if (qa > 0.0 && qa < 1e300) {
+        frexp(bound * qa, &e);
+        emax[k] = max(emax[k], e);
+      }
+    }
+  }
+}
+
+// A record is redone in FP64 when every pixel centre is near or beyond the
+// kernel edge (FP32 cancellation in 1 - u), when its FP32 sum is 0 (the
+// reference's fallback branch) or below 2^-40 (its per-cell factor numerator
+// / S would leave the FP32 range once scaled for the tile accumulators).
+__device__ __forceinline__ bool ill_conditioned(float S, float umin) {
+  return umin > 0.9f || !(S >= 0x1p-40f);
+}
+
+// Weight factor of a well-conditioned record from its compensated FP32 sum
+// S + S_err, by the one thread that holds it (weight numerator / S,
+// cic_2D.jl:187-188 and cic_3D.jl:168-169).
+__device__ __forceinline__ void finish_scalar(const TiledArgs& A, int64_t r, float S, float S_err, double& c_gm,
+                                              int* emax) {
+  const double Sd = (double)S + (double)S_err;
+  const double cpv = A.cp[r] / Sd;
+  c_gm += A.aux[r] * Sd;
+  store_factor(A, r, cpv, fabs(cpv), 0, emax);
+}
+
+// Ill-conditioned record (every pixel centre near or beyond the kernel edge,
+// or a zero FP32 sum): the reference's FP64 arithmetic with the whole warp,
+// as in the plain path, including its fallback when no centre is inside
+// (cic_2D.jl:196-205, cic_3D.jl:175-184).
 template <int DIMS, int KERN>
-__device__ void finish_record(const TiledArgs& A, int64_t r, float S, float S_err, float umin, int lane,
-                              bool overflow, double& c_gm, int* emax, unsigned long long* bacc) {
+__device__ void finish_fp64_warp(const TiledArgs& A, int64_t r, int lane, double& c_gm, int* emax) {
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
   const int njk = dm.y * dm.z;
   const int64_t F = (int64_t)dm.x * njk;
-  const int nch = A.pt.nq + 1;
-  if (A.det && lane == 0) {  // deterministic channel bounds (integer sums, flushed per warp)
-    const double num = fabs(A.cp[r]);
-    if (num > 0.0 && num < 1e300) {
-      for (int c = 0; c < nch; ++c) {
-        const double qa = c < A.pt.nq ? fabs((double)A.qv[(int64_t)c * A.cap + r]) : 1.0;
-        if (qa > 0.0 && qa < 1e300 && A.kexp[c] > -100000)
-          bacc[c] += (unsigned long long)ceil(ldexp(num * qa, 30 - A.kexp[c]));
-      }
+  PrepFP64 q;
+  prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
+  double s_w = 0.0, s_a = 0.0;
+  long long n_d = 0, n_t = 0;
+  for (int64_t f = lane; f < F; f += 32) {
+    const int a = (int)(f / njk);
+    const int rr = (int)(f - (int64_t)a * njk);
+    const int b = rr / dm.z, c = rr - b * dm.z;
+    double u, ar;
+    cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
+    s_a += ar;
+    n_t += 1;
+    if (u <= 1.0) {
+      s_w += shape_d<KERN>(A.kern, u) * q.knorm * ar;
+      n_d += 1;
     }
   }
-  double cpv = 0.0;
-  int fl = 0;
-  double bound = 0.0;  // largest per-cell weight of this particle
-  double gm = 0.0;
-  if (umin > 0.9f || !(S > 0.0f)) {
-    // ill-conditioned (every pixel centre near or beyond the kernel edge):
-    // the reference's FP64 arithmetic, as in the plain path
-    PrepFP64 q;
-    prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
-    double s_w = 0.0, s_a = 0.0;
-    long long n_d = 0, n_t = 0;
-    for (int64_t f = lane; f < F; f += 32) {
-      const int a = (int)(f / njk);
-      const int rr = (int)(f - (int64_t)a * njk);
-      const int b = rr / dm.z, c = rr - b * dm.z;
-      double u, ar;
-      cell_fp64<DIMS>(q, bx.x + a, bx.y + b, bx.z + c, &u, &ar);
-      s_a += ar;
-      n_t += 1;
-      if (u <= 1.0) {
-        s_w += shape_d<KERN>(A.kern, u) * q.knorm * ar;
-        n_d += 1;
-      }
-    }
-    s_w = warp_sum_d(s_w);
-    s_a = warp_sum_d(s_a);
-    n_d = warp_sum_ll(n_d);
-    n_t = warp_sum_ll(n_t);
+  s_w = warp_sum_d(s_w);
+  s_a = warp_sum_d(s_a);
+  n_d = warp_sum_ll(n_d);
+  n_t = warp_sum_ll(n_t);
+  if (lane == 0) {  // per-particle factors (the scalars of prep_bcast live on lane 0)
     const bool fallback = (s_w == 0.0);
-    fl = kRecFP64 | (fallback ? kRecFallback : 0);
-    if (lane == 0) {  // per-particle factors (the scalars of prep_bcast live on lane 0)
-      double wpp;
-      if (fallback) {
-        n_d = n_t;
-        wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
-      } else {
-        wpp = (double)n_d / s_w;
-      }
-      cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
-                      : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
-      bound = fabs(cpv) * (fallback ? 1.0 : q.knorm);
-      gm = q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    double wpp;
+    if (fallback) {
+      n_d = n_t;
+      wpp = s_a != 0.0 ? (double)n_d / s_a : 1.0;
+    } else {
+      wpp = (double)n_d / s_w;
     }
-  } else if (lane == 0) {  // FP64 on one lane: GB300's FP64 rate is a small fraction of FP32
-    const double Sd = (double)S + (double)S_err;
-    cpv = A.cp[r] / Sd;
-    bound = fabs(cpv);
-    gm = A.aux[r] * Sd;
-  }
-  if (lane == 0) {
-    A.cp[r] = cpv;
-    int ce = 0;
-    const float cm = (float)frexp(cpv, &ce);
-    A.cpm[r] = cm;
-    A.cpe[r] = ce;
-    if (fl) A.box[r].w = fl;
-    c_gm += gm;
-    int e;  // scale exponents per channel
-    if (bound > 0.0 && bound < 1e300) {
-      frexp(bound, &e);
-      emax[A.pt.nq] = max(emax[A.pt.nq], e);
-      for (int k = 0; k < A.pt.nq; ++k) {
-        const double qa = fabs((double)A.qv[(int64_t)k * A.cap + r]);
-        if (qa > 0.0 && qa < 1e300) {
-          frexp(bound * qa, &e);
-          emax[k] = max(emax[k], e);
-        }
-      }
-    }
-  }
-  if (!overflow) {  // tile lists
-    const int tx0 = bx.x / A.tdim[0], tx1 = (bx.x + dm.x - 1) / A.tdim[0];
-    const int ty0 = bx.y / A.tdim[1], ty1 = (bx.y + dm.y - 1) / A.tdim[1];
-    const int tz0 = bx.z / A.tdim[2], tz1 = (bx.z + dm.z - 1) / A.tdim[2];
-    const int nty = ty1 - ty0 + 1, ntz = tz1 - tz0 + 1;
-    const int nt = (tx1 - tx0 + 1) * nty * ntz;
-    for (int t = lane; t < nt; t += 32) {
-      const int ta = t / (nty * ntz), tb = (t / ntz) % nty, tc = t % ntz;
-      const int64_t tile = ((int64_t)(tx0 + ta) * A.ntile[1] + (ty0 + tb)) * A.ntile[2] + (tz0 + tc);
-      const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
-      A.pairs[slot] = (int)r;
-    }
+    const double cpv = DIMS == 2 ? q.area / (double)n_d * wpp * q.wgt * q.col
+                                 : q.vol / (double)n_d * wpp * q.wgt * A.mp.L;
+    c_gm += q.rho_in / (A.mp.L * A.mp.L * A.mp.L) * (fallback ? s_a : s_w);
+    store_factor(A, r, cpv, fabs(cpv) * (fallback ? 1.0 : q.knorm), kRecFP64 | (fallback ? kRecFallback : 0),
+                 emax);
   }
 }
 
-__device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int dims, double c_gm, const int* emax,
-                                            const unsigned long long* bacc) {
+// Tile-range of record r.
+struct TileSpan {
+  int tx0, ty0, tz0, nty, ntz, nt;
+};
+__device__ __forceinline__ TileSpan tile_span(const TiledArgs& A, int4 bx, int4 dm) {
+  TileSpan t;
+  t.tx0 = bx.x / A.tdim[0];
+  t.ty0 = bx.y / A.tdim[1];
+  t.tz0 = bx.z / A.tdim[2];
+  const int tx1 = (bx.x + dm.x - 1) / A.tdim[0];
+  const int ty1 = (bx.y + dm.y - 1) / A.tdim[1];
+  const int tz1 = (bx.z + dm.z - 1) / A.tdim[2];
+  t.nty = ty1 - t.ty0 + 1;
+  t.ntz = tz1 - t.tz0 + 1;
+  t.nt = (tx1 - t.tx0 + 1) * t.nty * t.ntz;
+  return t;
+}
+__device__ __forceinline__ void tile_entry(const TiledArgs& A, const TileSpan& s, int t, int r) {
+  const int ta = t / (s.nty * s.ntz), tb = (t / s.ntz) % s.nty, tc = t % s.ntz;
+  const int64_t tile = ((int64_t)(s.tx0 + ta) * A.ntile[1] + (s.ty0 + tb)) * A.ntile[2] + (s.tz0 + tc);
+  const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
+  A.pairs[slot] = r;
+}
+
+// Warp-wide channel maxima and sums before lane 0 flushes them.
+__device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int dims, double c_gm, int* emax) {
+  c_gm = warp_sum_d(c_gm);
+  for (int c = 0; c < A.pt.nq + 1; ++c) emax[c] = __reduce_max_sync(0xffffffffu, emax[c]);
   if (lane == 0) {
     if (dims == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
-    for (int c = 0; c < A.pt.nq + 1; ++c) {
+    for (int c = 0; c < A.pt.nq + 1; ++c)
       if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
-      if (bacc[c]) atomicAdd(&A.bsum[c], bacc[c]);
-    }
   }
 }
 
-// K3 body: the warp `wid` of `nw` takes the records with a footprint of at
-// most large_cells cells.
+// K3 body: the warp `wid` of `nw` takes groups of 32 consecutive records
+// (those with a footprint of at most large_cells cells).  The warp sums each
+// record's footprint together; lane j keeps record j's sum, and the 32 lanes
+// then finish their records side by side, so the FP64 division (a small
+// fraction of FP32 throughput on GB300) costs one warp instruction sequence
+// per 32 records.  Each lane also writes its record's tile-list entries.
 template <int DIMS, int KERN>
 __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int lane) {
   const int nrec = *A.n_rec;
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
-  unsigned long long bacc[kMaxQ + 1];
-  for (int c = 0; c <= A.pt.nq; ++c) {
-    emax[c] = INT_MIN;
-    bacc[c] = 0ull;
-  }
+  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
   __shared__ float2 tabs[8][3][kNormTab];  // one set per warp of a 256-thread CTA
   float2(*tab)[kNormTab] = tabs[(threadIdx.x >> 5) & 7];
-  for (int64_t r = wid; r < nrec; r += nw) {
-    const int4 dm = A.dimv[r];
-    const int64_t F = (int64_t)dm.x * dm.y * dm.z;
-    if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
-    float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-    if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab)
-      record_sum_tab<DIMS, KERN>(A.kern, A.geo[r], dm, lane, tab, s, comp, umin);
-    else
-      record_sum_fp32<DIMS, KERN>(A.kern, A.geo[r], dm, 0, F, lane, 32, s, comp, umin);
-    warp_reduce_comp(s, comp, umin);
-    finish_record<DIMS, KERN>(A, r, s, comp, umin, lane, overflow, c_gm, emax, bacc);
+  for (int64_t g0 = wid * 32; g0 < nrec; g0 += nw * 32) {
+    const int cnt = nrec - g0 < 32 ? (int)(nrec - g0) : 32;
+    float my_s = 0.0f, my_c = 0.0f, my_u = 0.0f;
+    bool mine = false;
+    for (int j = 0; j < cnt; ++j) {
+      const int4 dm = A.dimv[g0 + j];
+      const int64_t F = (int64_t)dm.x * dm.y * dm.z;
+      if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
+      float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
+      if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab)
+        record_sum_tab<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, lane, tab, s, comp, umin);
+      else
+        record_sum_fp32<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, 0, F, lane, 32, s, comp, umin);
+      warp_reduce_comp(s, comp, umin);
+      if (lane == j) {
+        my_s = s;
+        my_c = comp;
+        my_u = umin;
+        mine = true;
+      }
+    }
+    const int64_t r = g0 + lane;
+    const bool ill = mine && ill_conditioned(my_s, my_u);
+    for (unsigned m = __ballot_sync(0xffffffffu, ill); m; m &= m - 1)
+      finish_fp64_warp<DIMS, KERN>(A, g0 + __ffs(m) - 1, lane, c_gm, emax);
+    if (mine && !ill) finish_scalar(A, r, my_s, my_c, c_gm, emax);
+    if (mine && !overflow) {
+      const int4 bx = A.box[r];
+      const TileSpan sp = tile_span(A, bx, A.dimv[r]);
+      for (int t = 0; t < sp.nt; ++t) tile_entry(A, sp, t, (int)r);
+    }
   }
-  flush_stats(A, lane, DIMS, c_gm, emax, bacc);
+  flush_stats(A, lane, DIMS, c_gm, emax);
 }
 
-// K3: one warp per small record.
+// K3: one warp per group of 32 small records.
 template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
   norm_records<DIMS, KERN>(A, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
@@ -489,11 +499,7 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
-  unsigned long long bacc[kMaxQ + 1];
-  for (int c = 0; c <= A.pt.nq; ++c) {
-    emax[c] = INT_MIN;
-    bacc[c] = 0ull;
-  }
+  for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
   if (!overflow) {
     for (int64_t i = wid; i < nl; i += nw) {
       const int64_t r = A.large[i];
@@ -507,10 +513,15 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
         umin = fminf(umin, pv.z);
       }
       warp_reduce_comp(s, comp, umin);
-      finish_record<DIMS, KERN>(A, r, s, comp, umin, lane, overflow, c_gm, emax, bacc);
+      if (ill_conditioned(s, umin)) finish_fp64_warp<DIMS, KERN>(A, r, lane, c_gm, emax);
+      else if (lane == 0) finish_scalar(A, r, s, comp, c_gm, emax);
+      __syncwarp();
+      const int4 bx = A.box[r];
+      const TileSpan sp = tile_span(A, bx, A.dimv[r]);
+      for (int t = lane; t < sp.nt; t += 32) tile_entry(A, sp, t, (int)r);
     }
   }
-  flush_stats(A, lane, DIMS, c_gm, emax, bacc);
+  flush_stats(A, lane, DIMS, c_gm, emax);
 }
 
 template <int DIMS, int KERN>
@@ -538,6 +549,40 @@ __device__ __forceinline__ double cell_value(const float* hi, const float* lo, c
 // K4: one CTA per image tile.  DET selects exact int64 fixed-point tile sums
 // (bitwise reproducible) instead of TwoSum-compensated FP32 (hi, lo) pairs;
 // both use 8 bytes per channel and tile pixel.
+// Deposit of one (ill-conditioned record, tile) pair: per-cell weights in the
+// reference's FP64 arithmetic.  Kept out of line so that its FP64 state does
+// not raise the register demand of the FP32 cell loop.
+template <int DIMS, int KERN, int TY, int TZ, bool DET>
+__device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 bx, int4 dm, int a0, int b0, int c0,
+                                               int nb, int nc, int n, int la, int lb, int lc, int nq, int TV,
+                                               float* hi, float* lo, unsigned long long* fx, const double* s_scale,
+                                               int lane) {
+  PrepFP64 q;
+  prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
+  const bool fb = (bx.w & kRecFallback) != 0;
+  const double cpv = A.cp[r];
+  const double scw = s_scale[nq];
+  const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
+  for (int e = lane; e < n; e += 32) {
+    const int bc = fdiv(e, inv_nc);
+    const int c = e - bc * nc;
+    const int a = fdiv(bc, inv_nb);
+    const int b = bc - a * nb;
+    const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
+    double u, ar;
+    cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
+    const double wk = fb ? 1.0 : (u <= 1.0 ? shape_d<KERN>(A.kern, u) * q.knorm : 0.0);
+    const double pw = wk * ar * cpv;
+    if (pw != 0.0) {
+      const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+      acc_cell<DET>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
+      for (int k = 0; k < nq; ++k)
+        acc_cell<DET>(hi, lo, fx, k * TV + li,
+                      __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
+    }
+  }
+}
+
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw) {
   constexpr int TV = TX * TY * TZ;
@@ -551,26 +596,50 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
   const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
   for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
-  // channel scales (powers of two): 2^s_shift as double for the flush
-  __shared__ double s_scale[kMaxQ + 1];
-  __shared__ int s_shift[kMaxQ + 1];
-  if (threadIdx.x < nch) {
-    int sh;
-    if (DET) {
-      sh = fixed_exponent(A.kexp[threadIdx.x], A.bsum[threadIdx.x], *A.n_rec);
-    } else {
-      const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
-      sh = e < -100000 ? 0 : kScaleTop - e;
-    }
-    s_shift[threadIdx.x] = sh;
-    s_scale[threadIdx.x] = ldexp(1.0, sh);
-  }
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   // after an overflow of the pair list the lists are incomplete: deposit
   // nothing (the host grows the list and maps again)
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
+  // channel scales (powers of two): 2^s_shift as double for the flush
+  __shared__ double s_scale[kMaxQ + 1];
+  __shared__ int s_shift[kMaxQ + 1];
+  if (DET) {
+    // this tile's bound per channel: the sum over its pairs of the record's
+    // whole deposit (|numerator| * |q|), so every partial sum of the tile
+    // stays below 2^62 in int64 fixed point
+    __shared__ double s_bnd[kMaxQ + 1][8];
+    double bnd[kMaxQ + 1];
+    for (int c = 0; c < nch; ++c) bnd[c] = 0.0;
+    for (long long s = p0 + threadIdx.x; s < p1; s += blockDim.x) {
+      const int r = A.pairs[s];
+      const double tot = A.aux[r];
+      bnd[nq] += tot;
+      for (int k = 0; k < nq; ++k) bnd[k] += tot * fabs((double)A.qv[(int64_t)k * A.cap + r]);
+    }
+    for (int c = 0; c < nch; ++c) {
+      const double v = warp_sum_d(bnd[c]);
+      if (lane == 0) s_bnd[c][warp & 7] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nch) {
+      double b = 0.0;
+      for (int w = 0; w < (nwarp < 8 ? nwarp : 8); ++w) b += s_bnd[threadIdx.x][w];
+      // widened for the FP32 rounding of the cell values and of S
+      b *= 1.0 + 0x1p-18;
+      int e = 0;
+      if (b > 0.0 && b < 1e300) frexp(b, &e);  // b < 2^e
+      const int sh = (b > 0.0 && b < 1e300) ? 62 - e : 0;
+      s_shift[threadIdx.x] = sh;
+      s_scale[threadIdx.x] = ldexp(1.0, sh);
+    }
+  } else if (threadIdx.x < nch) {
+    const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
+    const int sh = e < -100000 ? 0 : kScaleTop - e;
+    s_shift[threadIdx.x] = sh;
+    s_scale[threadIdx.x] = ldexp(1.0, sh);
+  }
+  __syncthreads();
   const double scw = s_scale[nq];
   // per-warp axis tables of the current pair's intersection with the tile
   __shared__ float2 dtabs[8][3][32];
@@ -585,47 +654,35 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
     const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
     const int n = na * nb * nc;
-    const float inv_nc = 1.0f / (float)nc, inv_nb = 1.0f / (float)nb;
+    const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
     // local-frame offset of the tile origin
     const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
     if (bx.w & kRecFP64) {
-      // ill-conditioned particle: per-cell weights in the reference's FP64
-      PrepFP64 q;
-      prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
-      const bool fb = (bx.w & kRecFallback) != 0;
-      const double cpv = A.cp[r];
-      for (int e = lane; e < n; e += 32) {
-        const int bc = fdiv(e, inv_nc);
-        const int c = e - bc * nc;
-        const int a = fdiv(bc, inv_nb);
-        const int b = bc - a * nb;
-        const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
-        double u, ar;
-        cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
-        const double wk = fb ? 1.0 : (u <= 1.0 ? shape_d<KERN>(A.kern, u) * q.knorm : 0.0);
-        const double pw = wk * ar * cpv;
-        if (pw != 0.0) {
-          const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
-          acc_cell<DET>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
-          for (int k = 0; k < nq; ++k)
-            acc_cell<DET>(hi, lo, fx, k * TV + li,
-                          __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
-        }
-      }
+      deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, r, bx, dm, a0, b0, c0, nb, nc, n, la, lb, lc, nq, TV, hi, lo, fx,
+                                                 s_scale, lane);
       continue;
     }
     // per-record factors in FP32: cp = cpm * 2^cpe, shifted by the channel scale
     const float cpm = A.cpm[r];
     const int cpe = A.cpe[r];
-    const float cw = ldexpf(cpm, cpe + s_shift[nq]);
+    // (q is split into mantissa and exponent so no intermediate leaves the
+    // FP32 range: each factor is at most 2^62 / S of its channel's scale)
+    const float cw = cpm * pow2f(cpe + s_shift[nq]);
     float cq[NQ > 0 ? NQ : kMaxQ];
-    for (int k = 0; k < nq; ++k) cq[k] = ldexpf(cpm * A.qv[(int64_t)k * A.cap + r], cpe + s_shift[k]);
+    for (int k = 0; k < nq; ++k) {
+      float qm;
+      int qe;
+      split_f(A.qv[(int64_t)k * A.cap + r], qm, qe);
+      cq[k] = (cpm * qm) * pow2f(cpe + qe + s_shift[k]);
+    }
     const float4 g = A.geo[r];
     const float h = g.w, hinv = 1.0f / g.w;
-    for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms
-      if (i < na) tab[0][i] = axis_sq(g.x, h, a0 + i);
-      else if (i < na + nb) tab[1][i - na] = axis_sq(g.y, h, b0 + i - na);
-      else tab[2][i - na - nb] = DIMS == 3 ? axis_sq(g.z, h, c0 + i - na - nb) : make_float2(0.0f, 1.0f);
+    for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms; axis by selects
+      const int ax = i < na ? 0 : (i < na + nb ? 1 : 2);
+      const int k = i - (ax == 0 ? 0 : (ax == 1 ? na : na + nb));
+      const int c = k + (ax == 0 ? a0 : (ax == 1 ? b0 : c0));
+      tab[ax][k] = (DIMS == 2 && ax == 2) ? make_float2(0.0f, 1.0f)
+                                          : axis_sq(ax == 0 ? g.x : (ax == 1 ? g.y : g.z), h, c);
     }
     __syncwarp();
     const int lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
@@ -638,14 +695,12 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       const float u = u_of((ex.x + ey.x) + ez.x, hinv);
       if (u <= 1.0f) {
         const float gw = shape_f<KERN>(A.kern, u) * (ex.y * ey.y * ez.y);
-        if (gw != 0.0f) {
-          const int li = lbase + (a * TY + b) * TZ + c;
-          acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+        const int li = lbase + (a * TY + b) * TZ + c;
+        acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
-          for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
-            if (NQ == 0 && k >= nq) break;
-            acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
-          }
+        for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+          if (NQ == 0 && k >= nq) break;
+          acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
         }
       }
     }
