@@ -198,7 +198,7 @@ def bench_gpu(args):
     dev = torch.device("cuda", local)
     if args.batched_only:  # profiling runs: the batched workload alone
         import __graft_entry__ as graft
-        b = bench_batched(graft.load_package(), dev, args.steps, args.warmup)
+        b = bench_batched(graft.load_package(), dev, args.steps, args.warmup, args.batched_maps)
         if rank == 0:
             b.pop("rel_err_per_map")
             print(json.dumps(b), flush=True)
@@ -387,7 +387,7 @@ BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e
                   "autotuned tiles")
 
 
-def bench_batched(pkg, dev, steps, warmup):
+def bench_batched(pkg, dev, steps, warmup, n_maps=96):
     """The batched uneven-maps workload: maps/s of one graph-replayed batch
     against the plain FP64 method called map by map, and each map's error
     against the plain FP64 map (on pixels with W >= 1e-6 max W, relative to
@@ -395,7 +395,7 @@ def bench_batched(pkg, dev, steps, warmup):
     import torch
     from sphtogrid_gb300 import synth
     from sphtogrid_gb300.batch import MapSpec, SPHBatch
-    maps = synth.batched_2d()
+    maps = synth.batched_2d(n_maps=n_maps)
     specs, host = [], []
     for d in maps:
         par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["npix"])
@@ -513,7 +513,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched 96-map workload")
     ap.add_argument("--batched-only", action="store_true",
-                    help="time the batched 96-map workload alone (for profiler runs)")
+                    help="time the batched workload alone (for profiler runs)")
+    ap.add_argument("--batched-maps", type=int, default=96,
+                    help="maps in the batched workload (smaller for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

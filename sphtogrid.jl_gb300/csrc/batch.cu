@@ -97,11 +97,21 @@ __global__ void __launch_bounds__(256) kb_large_finish(BatchDev B) {
   }
 }
 
+// One tile of one map, for a compile-time channel count.  Out of line: the
+// persistent kernel dispatches among several specialisations, and a call per
+// tile keeps each one's register use inside its own cell loop.
+template <int DIMS, int NQ, int TX, int TY, int TZ, bool DET>
+__device__ __noinline__ void tile_call(const TiledArgs& A, long long t, unsigned char* smem_raw,
+                                       DepositShared& sh) {
+  deposit_tile<DIMS, -1, NQ, TX, TY, TZ, DET>(A, t, smem_raw, sh);
+}
+
 // The persistent deposit: every CTA takes the next tile from the queue until
 // the queue is empty.
 template <int TX, int TY, bool DET>
-__global__ void __launch_bounds__(256) kb_deposit(BatchDev B) {
+__global__ void __launch_bounds__(256, 4) kb_deposit(BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ DepositShared sh;
   __shared__ long long t_sh;
   for (;;) {
     if (threadIdx.x == 0) t_sh = (long long)atomicAdd(B.queue, 1ull);
@@ -112,8 +122,19 @@ __global__ void __launch_bounds__(256) kb_deposit(BatchDev B) {
     const int pos = find_seg_ll(B.tile_base, B.n_maps, t);
     const TiledArgs& A = B.maps[B.order[pos]];
     const long long local = t - B.tile_base[pos];
-    if (A.mp.dims == 2) deposit_tile<2, -1, 0, TX, TY, 1, DET>(A, local, smem_raw);
-    else deposit_tile<3, -1, 0, 8, 8, 8, DET>(A, local, smem_raw);
+    // the map's channel count as a compile-time constant keeps the per-pair
+    // factors in registers (3D maps carry one quantity)
+    if (A.mp.dims == 3) {
+      tile_call<3, 1, 8, 8, 8, DET>(A, local, smem_raw, sh);
+    } else {
+      switch (A.pt.nq) {
+        case 1: tile_call<2, 1, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+        case 2: tile_call<2, 2, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+        case 3: tile_call<2, 3, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+        case 4: tile_call<2, 4, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+        default: tile_call<2, 0, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+      }
+    }
   }
 }
 

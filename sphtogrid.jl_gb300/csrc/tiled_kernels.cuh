@@ -583,8 +583,17 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 b
   }
 }
 
+// Per-CTA scratch of the tile deposit besides the accumulators: one
+// instance per kernel, shared by every specialisation the kernel inlines.
+struct DepositShared {
+  double scale[kMaxQ + 1];  // 2^shift per channel, for the flush
+  int shift[kMaxQ + 1];
+  double bnd[kMaxQ + 1][8];  // deterministic mode: per-warp tile bounds
+  float2 tabs[8][3][32];     // per-warp axis tables of the current pair
+};
+
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-__device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw) {
+__device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh) {
   constexpr int TV = TX * TY * TZ;
   const int nq = NQ > 0 ? NQ : A.pt.nq;
   const int nch = nq + 1;
@@ -602,13 +611,13 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
   // channel scales (powers of two): 2^s_shift as double for the flush
-  __shared__ double s_scale[kMaxQ + 1];
-  __shared__ int s_shift[kMaxQ + 1];
+  double* s_scale = sh.scale;
+  int* s_shift = sh.shift;
   if (DET) {
     // this tile's bound per channel: the sum over its pairs of the record's
     // whole deposit (|numerator| * |q|), so every partial sum of the tile
     // stays below 2^62 in int64 fixed point
-    __shared__ double s_bnd[kMaxQ + 1][8];
+    double(*s_bnd)[8] = sh.bnd;
     double bnd[kMaxQ + 1];
     for (int c = 0; c < nch; ++c) bnd[c] = 0.0;
     for (long long s = p0 + threadIdx.x; s < p1; s += blockDim.x) {
@@ -642,8 +651,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   __syncthreads();
   const double scw = s_scale[nq];
   // per-warp axis tables of the current pair's intersection with the tile
-  __shared__ float2 dtabs[8][3][32];
-  float2(*tab)[32] = dtabs[warp & 7];
+  float2(*tab)[32] = sh.tabs[warp & 7];
   for (long long s = p0 + warp; s < p1; s += nwarp) {
     const int r = A.pairs[s];
     const int4 bx = A.box[r];
@@ -750,7 +758,8 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __global__ void __launch_bounds__(256, 4) k_deposit(TiledArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw);
+  __shared__ DepositShared sh;
+  deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw, sh);
 }
 
 template <int DIMS, int KERN, int NQ, bool DET>
