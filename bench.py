@@ -198,7 +198,8 @@ def bench_gpu(args):
     dev = torch.device("cuda", local)
     if args.batched_only:  # profiling runs: the batched workload alone
         import __graft_entry__ as graft
-        b = bench_batched(graft.load_package(), dev, args.steps, args.warmup, args.batched_maps)
+        b = bench_batched(graft.load_package(), dev, args.steps, args.warmup, args.batched_maps,
+                          args.deterministic)
         if rank == 0:
             b.pop("rel_err_per_map")
             print(json.dumps(b), flush=True)
@@ -361,6 +362,8 @@ def bench_gpu(args):
     }
     if other is not None:
         line["fp32c_other_mode"] = other
+    if rank == 0:
+        line["onchip_ceiling"] = _onchip_ceiling(L, ctx, _lib, value, other, args.deterministic)
     if batched is not None:
         line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -387,7 +390,7 @@ BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e
                   "autotuned tiles")
 
 
-def bench_batched(pkg, dev, steps, warmup, n_maps=96):
+def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False):
     """The batched uneven-maps workload: maps/s of one graph-replayed batch
     against the plain FP64 method called map by map, and each map's error
     against the plain FP64 map (on pixels with W >= 1e-6 max W, relative to
@@ -406,7 +409,7 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96):
         specs.append(MapSpec(tp, *ts, param=par, kernel=kern, dimensions=2))
         host.append((par, tp, ts, kern))
     t0 = time.perf_counter()
-    b = SPHBatch(specs)  # plans, autotunes and captures the graph
+    b = SPHBatch(specs, deterministic=deterministic)  # plans, autotunes, captures the graph
     plan_s = time.perf_counter() - t0
     for _ in range(warmup):
         b.launch()
@@ -459,9 +462,32 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96):
            "plain_fp64_maps_per_s": 1e3 * n / ms64, "speedup_vs_plain_fp64": ms64 / ms_batch,
            "rel_err_max": max(errs), "rel_err_median": float(np.median(errs)),
            "rel_err_per_map": [float(f"{e:.3g}") for e in errs],
-           "tuning": b.tuning, "plan_and_autotune_s": plan_s}
+           "deterministic": bool(deterministic), "tuning": b.tuning,
+           "plan_and_autotune_s": plan_s}
     b.close()
     return out
+
+
+def _onchip_ceiling(L, ctx, _lib, value, other, det):
+    """The deposit rate the shared-memory accumulation alone allows (3D map:
+    one quantity + the weight = 2 channel additions per deposit), from the
+    library's conflict-free microbenchmark, and the fraction reached."""
+    names = {0: "fp32_atomic_with_return", 1: "fp32_atomic_no_return", 2: "int64_atomic",
+             3: "fp32_compensated_add"}
+    rates = {}
+    for kind, nm in names.items():
+        r = C.c_double()
+        _lib.check(L.sphg_probe_smem_rate(ctx.handle, kind, C.byref(r)), ctx.handle)
+        rates[nm] = r.value
+    chans = 2
+    ceil_c = rates["fp32_compensated_add"] / chans
+    ceil_d = rates["int64_atomic"] / chans
+    v_c = value if not det else (other or {}).get("value")
+    v_d = value if det else (other or {}).get("value")
+    return {"smem_additions_per_s": rates, "channel_additions_per_deposit": chans,
+            "deposit_ceiling_fp32c": ceil_c, "deposit_ceiling_deterministic": ceil_d,
+            "frac_fp32c": (v_c / ceil_c) if v_c else None,
+            "frac_deterministic": (v_d / ceil_d) if v_d else None}
 
 
 def _rel_linf(a, b, floor=1e-9):

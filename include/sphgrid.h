@@ -217,6 +217,15 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
                  const sphg_particles *parts, const double *raw, const double *grad_out,
                  const sphg_grads *grads, void *stream);
 
+/* Measurement only (no counterpart in the reference): the rate, in additions
+ * per second over the whole GPU, of the shared-memory accumulation step of
+ * the tile deposit -- kind 0: FP32 atomic add with its old value used;
+ * 1: FP32 atomic add without return; 2: int64 atomic add (deterministic
+ * mode); 3: the compensated FP32 add (atomic add, TwoSum, error term into a
+ * second accumulator).  Conflict-free addresses: an upper bound, not a
+ * deposit rate.  Synchronous; allocates a few bytes of device memory. */
+int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);
+
 /* ------------------------------------------------------- no-allocation map
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: code running inside a host application that owns all device memory

@@ -20,6 +20,10 @@ def __getattr__(name):
     if name == "distributed_cic_map":
         from . import distributed
         return distributed.distributed_cic_map
+    if name in ("write_fits_image", "read_fits_image", "read_allsky_fits_image",
+                "write_vtk_image", "get_map_grid_2D", "get_map_grid_3D"):
+        from . import io
+        return getattr(io, name)
     if name == "SPHBatch" or name == "MapSpec":
         from . import batch
         return getattr(batch, name)

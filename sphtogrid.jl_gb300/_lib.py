@@ -172,6 +172,8 @@ def lib():
         L.sphg_adjoint.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
                                    C.POINTER(SphgParticles), vp, vp, C.POINTER(SphgGrads), vp]
         L.sphg_adjoint.restype = i32
+        L.sphg_probe_smem_rate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        L.sphg_probe_smem_rate.restype = i32
         L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]
         L.sphg_accumulate.restype = i32
         _lib = L

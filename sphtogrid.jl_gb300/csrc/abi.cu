@@ -575,6 +575,15 @@ int sphg_accumulate(sphg_context* ctx, int64_t len, const double* part, double* 
   return SPHG_OK;
 }
 
+int sphg_probe_smem_rate(sphg_context* ctx, int kind, double* ops_per_s) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!ops_per_s || kind < 0 || kind > 3) return fail(ctx, SPHG_ERR_ARG, "kind must be 0..3");
+  DeviceGuard g(ctx->device);
+  CK(sphg::probe_smem_rate(kind, ctx->num_sms, ctx->stream, ops_per_s));
+  return SPHG_OK;
+}
+
 int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
                  const sphg_particles* pt, const double* raw, const double* grad_out,
                  const sphg_grads* gr, void* stream) {

@@ -109,7 +109,7 @@ __device__ __noinline__ void tile_call(const TiledArgs& A, long long t, unsigned
 // The persistent deposit: every CTA takes the next tile from the queue until
 // the queue is empty.
 template <int TX, int TY, bool DET>
-__global__ void __launch_bounds__(256, 4) kb_deposit(BatchDev B) {
+__global__ void __launch_bounds__(256, 6) kb_deposit(BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DepositShared sh;
   __shared__ long long t_sh;

@@ -434,7 +434,7 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
 
 // K3: one warp per group of 32 small records.
 template <int DIMS, int KERN>
-__global__ void __launch_bounds__(256) k_norm_fill(TiledArgs A) {
+__global__ void __launch_bounds__(256, 4) k_norm_fill(TiledArgs A) {
   norm_records<DIMS, KERN>(A, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
                            ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
 }
@@ -756,7 +756,10 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-__global__ void __launch_bounds__(256, 4) k_deposit(TiledArgs A) {
+// Launch bounds by measurement: the deposit is latency-bound, so resident
+// warps matter more than the registers given up (3D: eight CTAs per SM;
+// 2D carries up to four channels per cell and keeps six).
+__global__ void __launch_bounds__(256, DIMS == 3 ? 8 : 6) k_deposit(TiledArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DepositShared sh;
   deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw, sh);
@@ -769,7 +772,7 @@ void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
     k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   } else {
-    constexpr int TX = 8, TY = 8, TZ = 8;
+    constexpr int TX = 16, TY = 8, TZ = 8;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
     k_deposit<3, KERN, NQ, TX, TY, TZ, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   }
