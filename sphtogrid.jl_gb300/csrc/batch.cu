@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256, 6) kb_deposit(BatchDev B) {
     // the map's channel count as a compile-time constant keeps the per-pair
     // factors in registers (3D maps carry one quantity)
     if (A.mp.dims == 3) {
-      tile_call<3, 1, 8, 8, 8, DET>(A, local, smem_raw, sh);
+      tile_call<3, 1, kTile3X, kTile3Y, kTile3Z, DET>(A, local, smem_raw, sh);
     } else {
       switch (A.pt.nq) {
         case 1: tile_call<2, 1, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
@@ -281,7 +281,8 @@ int build_plan(sphg_batch* b) {
     o.large = take(cap * sizeof(int));
     o.lstart = take((cap + 1) * sizeof(long long));
     o.part = take(M.chunk_cap * sizeof(float4));
-    const size_t tv = M.desc.opt.dimensions == 2 ? (size_t)p.tile_x * p.tile_y : 512;
+    const size_t tv = M.desc.opt.dimensions == 2 ? (size_t)p.tile_x * p.tile_y
+                                                 : (size_t)kTile3X * kTile3Y * kTile3Z;
     smem = std::max(smem, 2 * (size_t)(nq + 1) * tv * sizeof(float));
   }
   cudaError_t e = cudaMalloc(&p.mem, off);
@@ -359,7 +360,9 @@ int build_plan(sphg_batch* b) {
       A.tdim[1] = p.tile_y;
       A.tdim[2] = 1;
     } else {
-      A.tdim[0] = A.tdim[1] = A.tdim[2] = 8;
+      A.tdim[0] = kTile3X;
+      A.tdim[1] = kTile3Y;
+      A.tdim[2] = kTile3Z;
     }
     for (int d = 0; d < 3; ++d) A.ntile[d] = d < dims ? (int)((P + A.tdim[d] - 1) / A.tdim[d]) : 1;
     A.n_tiles = M.n_tiles;
@@ -585,7 +588,7 @@ int sphg_batch_create(sphg_context* ctx, int32_t n_maps, const sphg_map_desc* de
     for (sphg::BatchMapHost& M : b->maps) {
       const int dims = M.desc.opt.dimensions;
       const int64_t P = M.desc.par.Npixels[0];
-      const int tdx = dims == 2 ? c.tx : 8, tdy = dims == 2 ? c.ty : 8, tdz = dims == 2 ? 1 : 8;
+      const int tdx = dims == 2 ? c.tx : kTile3X, tdy = dims == 2 ? c.ty : kTile3Y, tdz = dims == 2 ? 1 : kTile3Z;
       M.n_tiles = ((P + tdx - 1) / tdx) * ((P + tdy - 1) / tdy) * (dims == 3 ? (P + tdz - 1) / tdz : 1);
       const int64_t n = M.desc.parts.n;
       if (M.pair_cap < 8 * n + M.n_tiles) M.pair_cap = 8 * n + M.n_tiles;
@@ -608,8 +611,8 @@ int sphg_batch_create(sphg_context* ctx, int32_t n_maps, const sphg_map_desc* de
     for (sphg::BatchMapHost& M : b->maps) {
       const int dims = M.desc.opt.dimensions;
       const int64_t P = M.desc.par.Npixels[0];
-      const int tdx = dims == 2 ? pick.tx : 8, tdy = dims == 2 ? pick.ty : 8;
-      M.n_tiles = ((P + tdx - 1) / tdx) * ((P + tdy - 1) / tdy) * (dims == 3 ? (P + 7) / 8 : 1);
+      const int tdx = dims == 2 ? pick.tx : kTile3X, tdy = dims == 2 ? pick.ty : kTile3Y;
+      M.n_tiles = ((P + tdx - 1) / tdx) * ((P + tdy - 1) / tdy) * (dims == 3 ? (P + kTile3Z - 1) / kTile3Z : 1);
     }
     if (int st = sphg::build_plan(b)) return done(st);
     if (int st = sphg::run_sized(b)) return done(st);

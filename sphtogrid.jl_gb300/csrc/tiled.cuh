@@ -40,6 +40,10 @@ constexpr int64_t kChunkCells = 4096;
 // brought to about 2^kScaleTop before it enters FP32 accumulators.
 constexpr int kScaleTop = 24;
 
+// 3D deposit tile (cells per axis), shared by the single-map and batched
+// paths so that deterministic sums agree bit for bit between them.
+constexpr int kTile3X = 16, kTile3Y = 8, kTile3Z = 8;
+
 struct TiledArgs {
   DevParticles pt;
   DevMapParams mp;

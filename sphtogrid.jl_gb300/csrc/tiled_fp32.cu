@@ -33,7 +33,7 @@ void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_t
   if (dims == 2) {
     tdim[0] = 16; tdim[1] = 16; tdim[2] = 1;
   } else {
-    tdim[0] = 16; tdim[1] = 8; tdim[2] = 8;  // matches the 3D deposit launch
+    tdim[0] = kTile3X; tdim[1] = kTile3Y; tdim[2] = kTile3Z;
   }
   for (int d = 0; d < 3; ++d) ntile[d] = (d < dims) ? (int)((P + tdim[d] - 1) / tdim[d]) : 1;
   *n_tiles = (int64_t)ntile[0] * ntile[1] * ntile[2];

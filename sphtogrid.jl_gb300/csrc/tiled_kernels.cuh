@@ -772,7 +772,7 @@ void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
     k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   } else {
-    constexpr int TX = 16, TY = 8, TZ = 8;
+    constexpr int TX = kTile3X, TY = kTile3Y, TZ = kTile3Z;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
     k_deposit<3, KERN, NQ, TX, TY, TZ, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   }
