@@ -42,7 +42,7 @@ constexpr int kScaleTop = 24;
 
 // 3D deposit tile (cells per axis), shared by the single-map and batched
 // paths so that deterministic sums agree bit for bit between them.
-constexpr int kTile3X = 16, kTile3Y = 8, kTile3Z = 8;
+constexpr int kTile3X = 8, kTile3Y = 8, kTile3Z = 8;
 
 struct TiledArgs {
   DevParticles pt;

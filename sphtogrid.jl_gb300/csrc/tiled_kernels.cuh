@@ -188,10 +188,31 @@ __device__ __forceinline__ void record_sum_fp32(int kern, const float4 g, const 
 // side at most kNormTab cells).
 constexpr int kNormTab = 64;
 
-// The whole footprint of one record from per-axis tables filled by the warp.
+// 3D footprints with at most this many (x, y) columns also get a per-warp
+// plane table.
+constexpr int kNormPlane = 256;
+
+// A cell from its (x, y) plane entry {sx + sy, ox * oy} and its z term: the
+// same operations in the same order as cell_term, so the same u and weight.
+template <int DIMS, int KERN>
+__device__ __forceinline__ void cell_term_plane(int kern, float2 pxy, float2 ez, float hinv, float& s,
+                                                float& comp, float& umin) {
+  const float u = u_of(pxy.x + ez.x, hinv);
+  umin = fminf(umin, u);
+  if (u <= 1.0f) {
+    float t, e;
+    two_sum(s, shape_f<KERN>(kern, u) * (pxy.y * ez.y), t, e);
+    s = t;
+    comp += e;
+  }
+}
+
+// The whole footprint of one record from per-axis tables filled by the warp
+// (3D footprints with few columns: from a plane table too, one index
+// division per cell instead of two).
 template <int DIMS, int KERN>
 __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const int4 dm, int lane, float2 (*tab)[kNormTab],
-                                               float& s, float& comp, float& umin) {
+                                               float2* plane, float& s, float& comp, float& umin) {
   const float h = g.w, hinv = 1.0f / g.w;
   const int ntab = dm.x + dm.y + (DIMS == 3 ? dm.z : 0);
   for (int i = lane; i < ntab; i += 32) {  // axis and offset by selects (no divergence)
@@ -200,6 +221,24 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
     tab[ax][k] = axis_sq(ax == 0 ? g.x : (ax == 1 ? g.y : g.z), h, k);
   }
   __syncwarp();
+  if (DIMS == 3 && dm.x * dm.y <= kNormPlane) {
+    const int nab = dm.x * dm.y;
+    const float inv_ny = inv_small(dm.y);
+    for (int i = lane; i < nab; i += 32) {
+      const int a = fdiv(i, inv_ny), b = i - a * dm.y;
+      const float2 ex = tab[0][a], ey = tab[1][b];
+      plane[i] = make_float2(ex.x + ey.x, ex.y * ey.y);
+    }
+    __syncwarp();
+    const int F = nab * dm.z;
+    const float inv_nz = inv_small(dm.z);
+    for (int f = lane; f < F; f += 32) {
+      const int ab = fdiv(f, inv_nz), c = f - ab * dm.z;
+      cell_term_plane<DIMS, KERN>(kern, plane[ab], tab[2][c], hinv, s, comp, umin);
+    }
+    __syncwarp();  // the tables are refilled for the next record
+    return;
+  }
   const int njk = dm.y * dm.z;
   const int F = dm.x * njk;
   const float inv_njk = inv_small(njk), inv_nz = inv_small(dm.z);
@@ -396,7 +435,9 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
   int emax[kMaxQ + 1];
   for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
   __shared__ float2 tabs[8][3][kNormTab];  // one set per warp of a 256-thread CTA
+  __shared__ float2 planes[8][DIMS == 3 ? kNormPlane : 1];
   float2(*tab)[kNormTab] = tabs[(threadIdx.x >> 5) & 7];
+  float2* plane = planes[(threadIdx.x >> 5) & 7];
   for (int64_t g0 = wid * 32; g0 < nrec; g0 += nw * 32) {
     const int cnt = nrec - g0 < 32 ? (int)(nrec - g0) : 32;
     float my_s = 0.0f, my_c = 0.0f, my_u = 0.0f;
@@ -407,7 +448,7 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
       if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
       float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
       if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab)
-        record_sum_tab<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, lane, tab, s, comp, umin);
+        record_sum_tab<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, lane, tab, plane, s, comp, umin);
       else
         record_sum_fp32<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, 0, F, lane, 32, s, comp, umin);
       warp_reduce_comp(s, comp, umin);
@@ -585,12 +626,71 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 b
 
 // Per-CTA scratch of the tile deposit besides the accumulators: one
 // instance per kernel, shared by every specialisation the kernel inlines.
+// Pairs a warp prepares together (one lane each) before depositing them.
+constexpr int kPairBatch = 16;
+// Channels whose per-pair factors the header holds (more: recomputed).
+constexpr int kHdrQ = 4;
+
+// One (record, tile) pair as the deposit consumes it: its intersection
+// with the tile, the record's position offsets and FP32 factors.
+struct PairHdr {
+  int a0, b0, c0;  // intersection start, footprint-local
+  int dims;        // na | nb << 8 | nc << 16 | FP64-record flag << 24
+  int lbase;       // tile-local cell of the intersection start
+  int r;           // record
+  float fx, fy, fz, h, hinv, cw;
+  float cq[kHdrQ];
+};
+
 struct DepositShared {
-  double scale[kMaxQ + 1];  // 2^shift per channel, for the flush
+  double scale[kMaxQ + 1];  // 2^shift per channel
+  double unscale[kMaxQ + 1];  // 2^-shift per channel, for the flush (exact)
   int shift[kMaxQ + 1];
   double bnd[kMaxQ + 1][8];  // deterministic mode: per-warp tile bounds
   float2 tabs[8][3][32];     // per-warp axis tables of the current pair
+  PairHdr hdr[8][kPairBatch];  // per-warp batch of prepared pairs
 };
+
+// FP32 factor of channel k of record r: cpm * q * 2^(cpe + shift), with q
+// split into mantissa and exponent so no intermediate leaves the FP32 range
+// (each factor is at most 2^62 / S of its channel's scale).
+__device__ __forceinline__ float channel_factor(const TiledArgs& A, int r, int k, float cpm, int cpe, int shift) {
+  float qm;
+  int qe;
+  split_f(A.qv[(int64_t)k * A.cap + r], qm, qe);
+  return (cpm * qm) * pow2f(cpe + qe + shift);
+}
+
+// Phase A of the deposit: one lane prepares pair (record r, tile at
+// ox, oy, oz) into `H`.
+template <int DIMS, int NQ, int TX, int TY, int TZ>
+__device__ __forceinline__ void prepare_pair(const TiledArgs& A, int r, int ox, int oy, int oz, int nq,
+                                             const int* s_shift, PairHdr& H) {
+  const int4 bx = A.box[r];
+  const int4 dm = A.dimv[r];
+  const int a0 = max(0, ox - bx.x), a1 = min(dm.x, ox + TX - bx.x);
+  const int b0 = max(0, oy - bx.y), b1 = min(dm.y, oy + TY - bx.y);
+  const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
+  const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
+  H.a0 = a0;
+  H.b0 = b0;
+  H.c0 = c0;
+  H.dims = (a1 - a0) | ((b1 - b0) << 8) | ((c1 - c0) << 16) | ((bx.w & kRecFP64) ? (1 << 24) : 0);
+  H.lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
+  H.r = r;
+  if (bx.w & kRecFP64) return;
+  const float4 g = A.geo[r];
+  H.fx = g.x;
+  H.fy = g.y;
+  H.fz = g.z;
+  H.h = g.w;
+  H.hinv = 1.0f / g.w;
+  const float cpm = A.cpm[r];
+  const int cpe = A.cpe[r];
+  H.cw = cpm * pow2f(cpe + s_shift[nq]);
+  if (NQ > 0 && NQ <= kHdrQ)
+    for (int k = 0; k < NQ; ++k) H.cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
+}
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh) {
@@ -612,6 +712,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
   // channel scales (powers of two): 2^s_shift as double for the flush
   double* s_scale = sh.scale;
+  double* s_unscale = sh.unscale;
   int* s_shift = sh.shift;
   if (DET) {
     // this tile's bound per channel: the sum over its pairs of the record's
@@ -641,84 +742,92 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       const int sh = (b > 0.0 && b < 1e300) ? 62 - e : 0;
       s_shift[threadIdx.x] = sh;
       s_scale[threadIdx.x] = ldexp(1.0, sh);
+      s_unscale[threadIdx.x] = ldexp(1.0, -sh);
     }
   } else if (threadIdx.x < nch) {
     const int e = A.exps[threadIdx.x];  // initialised far below any real exponent
     const int sh = e < -100000 ? 0 : kScaleTop - e;
     s_shift[threadIdx.x] = sh;
     s_scale[threadIdx.x] = ldexp(1.0, sh);
+    s_unscale[threadIdx.x] = ldexp(1.0, -sh);
   }
   __syncthreads();
-  const double scw = s_scale[nq];
   // per-warp axis tables of the current pair's intersection with the tile
   float2(*tab)[32] = sh.tabs[warp & 7];
-  for (long long s = p0 + warp; s < p1; s += nwarp) {
-    const int r = A.pairs[s];
-    const int4 bx = A.box[r];
-    const int4 dm = A.dimv[r];
-    // intersection of the footprint with the tile, in footprint-local indices
-    const int a0 = max(0, ox - bx.x), a1 = min(dm.x, ox + TX - bx.x);
-    const int b0 = max(0, oy - bx.y), b1 = min(dm.y, oy + TY - bx.y);
-    const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
-    const int na = a1 - a0, nb = b1 - b0, nc = c1 - c0;
-    const int n = na * nb * nc;
-    const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
-    // local-frame offset of the tile origin
-    const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
-    if (bx.w & kRecFP64) {
-      deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, r, bx, dm, a0, b0, c0, nb, nc, n, la, lb, lc, nq, TV, hi, lo, fx,
-                                                 s_scale, lane);
-      continue;
-    }
-    // per-record factors in FP32: cp = cpm * 2^cpe, shifted by the channel scale
-    const float cpm = A.cpm[r];
-    const int cpe = A.cpe[r];
-    // (q is split into mantissa and exponent so no intermediate leaves the
-    // FP32 range: each factor is at most 2^62 / S of its channel's scale)
-    const float cw = cpm * pow2f(cpe + s_shift[nq]);
-    float cq[NQ > 0 ? NQ : kMaxQ];
-    for (int k = 0; k < nq; ++k) {
-      float qm;
-      int qe;
-      split_f(A.qv[(int64_t)k * A.cap + r], qm, qe);
-      cq[k] = (cpm * qm) * pow2f(cpe + qe + s_shift[k]);
-    }
-    const float4 g = A.geo[r];
-    const float h = g.w, hinv = 1.0f / g.w;
-    for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms; axis by selects
-      const int ax = i < na ? 0 : (i < na + nb ? 1 : 2);
-      const int k = i - (ax == 0 ? 0 : (ax == 1 ? na : na + nb));
-      const int c = k + (ax == 0 ? a0 : (ax == 1 ? b0 : c0));
-      tab[ax][k] = (DIMS == 2 && ax == 2) ? make_float2(0.0f, 1.0f)
-                                          : axis_sq(ax == 0 ? g.x : (ax == 1 ? g.y : g.z), h, c);
-    }
+  PairHdr* hdr = sh.hdr[warp & 7];
+  // The warp's pairs are p0 + warp + j * nwarp.  Phase A: each of kPairBatch
+  // lanes prepares one pair of the next batch (their record loads are in
+  // flight together, and the per-pair arithmetic runs once per batch);
+  // phase B: the warp deposits the batch pair by pair from the headers.
+  for (long long sb = p0 + warp; sb < p1; sb += (long long)nwarp * kPairBatch) {
+    const long long sj = sb + (long long)lane * nwarp;
+    if (lane < kPairBatch && sj < p1)
+      prepare_pair<DIMS, NQ, TX, TY, TZ>(A, A.pairs[sj], ox, oy, oz, nq, s_shift, hdr[lane]);
     __syncwarp();
-    const int lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
-    for (int e = lane; e < n; e += 32) {
-      const int bc = fdiv(e, inv_nc);
-      const int c = e - bc * nc;
-      const int a = fdiv(bc, inv_nb);
-      const int b = bc - a * nb;
-      const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
-      const float u = u_of((ex.x + ey.x) + ez.x, hinv);
-      if (u <= 1.0f) {
-        const float gw = shape_f<KERN>(A.kern, u) * (ex.y * ey.y * ez.y);
-        const int li = lbase + (a * TY + b) * TZ + c;
-        acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+    const long long left = (p1 - sb + nwarp - 1) / nwarp;
+    const int cnt = left < kPairBatch ? (int)left : kPairBatch;
+    for (int j = 0; j < cnt; ++j) {
+      const PairHdr& H = hdr[j];
+      const int dims = H.dims;
+      const int na = dims & 0xff, nb = (dims >> 8) & 0xff, nc = (dims >> 16) & 0xff;
+      const int n = na * nb * nc;
+      const int a0 = H.a0, b0 = H.b0, c0 = H.c0;
+      if (dims & (1 << 24)) {
+        const int r = H.r;
+        const int4 bx = A.box[r];
+        const int4 dm = A.dimv[r];
+        const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
+        deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, r, bx, dm, a0, b0, c0, nb, nc, n, la, lb, lc, nq, TV, hi, lo,
+                                                   fx, s_scale, lane);
+      } else {
+        const float h = H.h, hinv = H.hinv, cw = H.cw;
+        float cq[NQ > 0 ? NQ : kMaxQ];
+        if (NQ > 0 && NQ <= kHdrQ) {
+          for (int k = 0; k < nq; ++k) cq[k] = H.cq[k];
+        } else {  // more channels than the header holds
+          const int r = H.r;
+          const float cpm = A.cpm[r];
+          const int cpe = A.cpe[r];
+          for (int k = 0; k < nq; ++k) cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
+        }
+        for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms; axis by selects
+          const int ax = i < na ? 0 : (i < na + nb ? 1 : 2);
+          const int k = i - (ax == 0 ? 0 : (ax == 1 ? na : na + nb));
+          const int c = k + (ax == 0 ? a0 : (ax == 1 ? b0 : c0));
+          tab[ax][k] = (DIMS == 2 && ax == 2) ? make_float2(0.0f, 1.0f)
+                                              : axis_sq(ax == 0 ? H.fx : (ax == 1 ? H.fy : H.fz), h, c);
+        }
+        __syncwarp();
+        const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
+        const int lbase = H.lbase;
+        for (int e = lane; e < n; e += 32) {
+          const int bc = fdiv(e, inv_nc);
+          const int c = e - bc * nc;
+          const int a = fdiv(bc, inv_nb);
+          const int b = bc - a * nb;
+          const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
+          const float u = u_of((ex.x + ey.x) + ez.x, hinv);
+          if (u <= 1.0f) {
+            const float gw = shape_f<KERN>(A.kern, u) * (ex.y * ey.y * ez.y);
+            const int li = lbase + (a * TY + b) * TZ + c;
+            acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
-        for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
-          if (NQ == 0 && k >= nq) break;
-          acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
+            for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+              if (NQ == 0 && k >= nq) break;
+              acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
+            }
+          }
         }
       }
+      __syncwarp();  // the tables are refilled for the next pair
     }
-    __syncwarp();  // the tables are refilled for the next pair
+    __syncwarp();  // the headers are refilled for the next batch
   }
   __syncthreads();
   // flush: FP64 values straight into the output layout
   const int64_t P = A.mp.P;
   const int64_t PD = DIMS == 2 ? P * P : P * P * P;
-  const double inv_w = 1.0 / scw;
+  const double inv_w = s_unscale[nq];
   for (int v = threadIdx.x; v < TV; v += blockDim.x) {
     int li, i, j, k;
     if (DIMS == 2 && A.mode == 0) {
@@ -739,14 +848,14 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     if (A.mode == 1) {  // raw (P^D, nq+1) accumulator
       const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
       A.out[row + (int64_t)nq * PD] = W;
-      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
+      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c];
     } else if (DIMS == 3) {
-      double Q = cell_value<DET>(hi, lo, fx, li) / s_scale[0];
+      double Q = cell_value<DET>(hi, lo, fx, li) * s_unscale[0];
       if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
       A.out[((int64_t)i * P + j) * P + k] = Q;
     } else {
       for (int c = 0; c < nq; ++c) {
-        double Q = cell_value<DET>(hi, lo, fx, c * TV + li) / s_scale[c];
+        double Q = cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c];
         if (A.reduce && W > 0.0) Q /= W;
         A.out[(int64_t)i + P * j + PD * c] = Q;
       }
