@@ -198,8 +198,9 @@ def bench_gpu(args):
     dev = torch.device("cuda", local)
     if args.batched_only:  # profiling runs: the batched workload alone
         import __graft_entry__ as graft
+        tun = tuple(int(x) for x in args.batched_tuning.split(",")) if args.batched_tuning else None
         b = bench_batched(graft.load_package(), dev, args.steps, args.warmup, args.batched_maps,
-                          args.deterministic)
+                          args.deterministic, tun)
         if rank == 0:
             b.pop("rel_err_per_map")
             print(json.dumps(b), flush=True)
@@ -390,7 +391,7 @@ BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e
                   "autotuned tiles")
 
 
-def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False):
+def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tuning=None):
     """The batched uneven-maps workload: maps/s of one graph-replayed batch
     against the plain FP64 method called map by map, and each map's error
     against the plain FP64 map (on pixels with W >= 1e-6 max W, relative to
@@ -409,7 +410,8 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False):
         specs.append(MapSpec(tp, *ts, param=par, kernel=kern, dimensions=2))
         host.append((par, tp, ts, kern))
     t0 = time.perf_counter()
-    b = SPHBatch(specs, deterministic=deterministic)  # plans, autotunes, captures the graph
+    # plans, autotunes (unless the tuning is given) and captures the graph
+    b = SPHBatch(specs, deterministic=deterministic, tuning=tuning)
     plan_s = time.perf_counter() - t0
     for _ in range(warmup):
         b.launch()
@@ -542,6 +544,8 @@ def main():
                     help="time the batched workload alone (for profiler runs)")
     ap.add_argument("--batched-maps", type=int, default=96,
                     help="maps in the batched workload (smaller for profiler captures)")
+    ap.add_argument("--batched-tuning", default=None,
+                    help="tile_x,tile_y,ctas_per_sm,large_cells instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)
