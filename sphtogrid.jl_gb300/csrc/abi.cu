@@ -412,9 +412,10 @@ again:
   mp.boxsize = par->boxsize;
   mp.periodic = par->periodic;
   mp.center_mode = opt->center;
-  // a re-run after K1 already centred the caller's device positions in place
-  // must not centre again (host inputs are copied afresh on every pass)
-  if (rerun && !host && opt->center == SPHG_CENTER_INPLACE) mp.center_mode = SPHG_CENTER_NONE;
+  // a re-run must not centre again: K1 already centred the caller's
+  // positions in place (device inputs), or the first pass wrote the centred
+  // positions back into the caller's host array, from which they are copied
+  if (rerun && opt->center == SPHG_CENTER_INPLACE) mp.center_mode = SPHG_CENTER_NONE;
   mp.filter = opt->filter;
   mp.calc_mean = dims == 2 ? opt->calc_mean : 0;  // cic_mapping_3D gets no calc_mean (:219)
   mp.kernel_dim = opt->kernel_dim;

@@ -88,7 +88,7 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
                reduce_image: bool = True, return_both_maps: bool = False, dimensions: int = 2,
                calc_mean: bool = False, stokes: bool = False, sort_z: bool = False,
                precision: str = "fp64", deterministic: bool = False, device: int = 0,
-               return_stats: bool = False, center_in_place: bool = True):
+               return_stats: bool = False, center_in_place: bool = True, context=None):
     """Map particle quantities to a 2D projected or 3D gridded image.
 
     Arguments and keywords are those of the reference; ``parallel`` is
@@ -97,7 +97,8 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     with compensated sums), ``deterministic`` (bitwise reproducible sums),
     ``device`` (host inputs: which GPU), ``return_stats`` (also return a dict
     with particle / deposit counts and the 3D mass diagnostic),
-    ``center_in_place`` (False: centre on the fly and leave ``Pos`` as it is).
+    ``center_in_place`` (False: centre on the fly and leave ``Pos`` as it is),
+    ``context`` (a ``Context`` to map in instead of the device's default one).
     """
     if RM is not None or stokes:
         raise NotImplementedError(
@@ -114,11 +115,11 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     if on_device:
         out = _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image,
                          return_both_maps, dimensions, calc_mean, sort_z, precision, deterministic,
-                         center_in_place)
+                         center_in_place, context)
     else:
         out = _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image,
                          return_both_maps, dimensions, calc_mean, sort_z, precision, deterministic,
-                         device, center_in_place)
+                         device, center_in_place, context)
     image, stats = out
     if show_progress:
         log.info("sphMapping: %d / %d particles mapped, %d deposits, %.3f s",
@@ -126,7 +127,8 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
     return (image, stats) if return_stats else image
 
 def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
-               dims, calc_mean, sort_z, precision, deterministic, device, center_in_place=True):
+               dims, calc_mean, sort_z, precision, deterministic, device, center_in_place=True,
+               context=None):
     if not isinstance(Pos, np.ndarray) or Pos.ndim != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) array")
     n = Pos.shape[1]
@@ -195,7 +197,7 @@ def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
     else:
         pt.q_stride_p, pt.q_stride_k = q.strides[1] // q.itemsize, q.strides[0] // q.itemsize
     st = _lib.SphgStats()
-    ctx = _lib.default_context(device)
+    ctx = context if context is not None else _lib.default_context(device)
     _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
                                    flat.ctypes.data, None, C.byref(st)), ctx.handle)
     if writeback is not None:
@@ -220,7 +222,7 @@ def _torch_dt(t):
     raise TypeError(f"unsupported dtype {t.dtype}")
 
 def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
-               dims, calc_mean, sort_z, precision, deterministic, center_in_place=True):
+               dims, calc_mean, sort_z, precision, deterministic, center_in_place=True, context=None):
     import torch
     if Pos.dim() != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) tensor")
@@ -258,7 +260,7 @@ def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
     else:
         pt.q_stride_p, pt.q_stride_k = q.stride(1), q.stride(0)
     st = _lib.SphgStats()
-    ctx = _lib.default_context(dev.index if dev.index is not None else 0)
+    ctx = context if context is not None else _lib.default_context(dev.index if dev.index is not None else 0)
     stream = _lib.stream_handle(torch.cuda.current_stream(dev))
     _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
                                    C.c_void_p(flat.data_ptr()), stream, C.byref(st)),

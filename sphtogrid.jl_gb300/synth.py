@@ -128,3 +128,47 @@ def batched_2d(n_maps=96, seed=0, dtype=np.float32, n_min=10_000, n_max=2_000_00
              "limits": (0.0, 1.0), "npix": P, "kernel": kernel, "dims": 2}
         maps.append(d)
     return maps
+
+
+def _lognormal_field(ng, sigma_ln, slope, rng):
+    """Density field on an ng^3 periodic grid: exp of a Gaussian random field
+    with power spectrum P(k) ∝ k^slope, scaled to a standard deviation of
+    sigma_ln in ln rho, normalised to mean 1."""
+    kx = np.fft.fftfreq(ng) * ng
+    kz = np.fft.rfftfreq(ng) * ng
+    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
+    amp = np.zeros_like(k2)
+    nz = k2 > 0
+    amp[nz] = k2[nz] ** (slope / 4.0)  # sqrt(P(k)), P ∝ |k|^slope
+    noise = rng.standard_normal((ng, ng, ng // 2 + 1)) + 1j * rng.standard_normal((ng, ng, ng // 2 + 1))
+    delta = np.fft.irfftn(noise * amp, s=(ng, ng, ng))
+    delta *= sigma_ln / delta.std()
+    rho = np.exp(delta)
+    return rho / rho.mean()
+
+
+def large_hdr_2d(N=2 ** 27, npix=4096, seed=0, dtype=np.float32, seed_grid=512, sigma_ln=2.0,
+                 slope=-3.0, h_min=1e-4, h_max=0.2, n_ngb=64):
+    """Large high-dynamic-range projection: particles in the periodic unit box
+    sampled ∝ a log-normal density field (sigma_ln 2, P(k) ∝ k^-3 on a
+    seed_grid^3 grid; per-cell counts Poisson with mean N * mass fraction, so
+    the total is N up to Poisson noise), positions uniform inside their cell,
+    hsml = (3 n_ngb / (4 pi N rho))^(1/3) from the cell's density clipped to
+    [h_min, h_max] (three decades), mass 1/N, Bin_Quant = Weights = rho,
+    Cubic kernel, 2D map of npix^2 over the unit box."""
+    rng = np.random.default_rng(seed)
+    rho_c = _lognormal_field(seed_grid, sigma_ln, slope, rng).reshape(-1)
+    counts = rng.poisson(N * rho_c / rho_c.sum())
+    cell = np.repeat(np.arange(rho_c.size, dtype=np.int64), counts)
+    n = cell.size
+    g = seed_grid
+    ijk = np.stack([cell // (g * g), (cell // g) % g, cell % g]).astype(np.float64)
+    pos = (ijk + rng.random((3, n))) / g
+    rho = rho_c[cell]
+    hsml = np.clip((3.0 * n_ngb / (4.0 * math.pi * n * rho)) ** (1.0 / 3.0), h_min, h_max)
+    d = {"pos": _julia_pos(pos.astype(dtype)), "hsml": hsml.astype(dtype),
+         "mass": np.full(n, 1.0 / n, dtype=dtype), "rho": rho.astype(dtype)}
+    d["bin_q"] = d["rho"]
+    d["weights"] = d["rho"]
+    d.update(limits=(0.0, 1.0), npix=npix, kernel="cubic", dims=2, boxsize=1.0)
+    return d

@@ -463,3 +463,46 @@ def test_deterministic_full_size_2d(gpu, oracle):
     ref, _ = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["mass"], d["rho"],
                                 d["bin_q"], d["weights"], param=opar, kernel="cubic", kernel_dim=2)
     assert rel_linf(outs[0], ref, FLOOR) <= TOL["fp32c"]
+
+
+@pytest.mark.parametrize("on_device", [False, True])
+@pytest.mark.parametrize("det", [False, True])
+def test_overflow_rerun_centres_once(gpu, oracle, on_device, det):
+    """A fresh context's tile-pair list is sized for 8 pairs per particle;
+    particles of h = 0.3 on a 256^2 map overlap ~100 tiles each, so the first
+    pass overflows and the map is run again with a grown list.  The re-run
+    must give the oracle's map and leave the caller's positions centred once
+    (SPHG_CENTER_INPLACE), for host and device inputs."""
+    import torch
+    rng = np.random.default_rng(11)
+    n = 1500
+    pos = np.asfortranarray(rng.uniform(2.0, 4.0, (3, n)))
+    hsml = np.full(n, 0.3)
+    m = rng.uniform(0.5, 1.5, n) / n
+    rho = rng.uniform(0.5, 2.0, n)
+    q = rng.uniform(0.5, 2.0, n)
+    kw = dict(center=[3.0, 3.0, 3.0], x_size=2.0, y_size=2.0, z_size=2.0, Npixels=256)
+    opar = oracle.mapping_parameters(**kw)
+    ref, info = oracle.sph_mapping(pos, hsml, m, rho, q, rho, param=opar, kernel="cubic",
+                                   copy_pos=True)
+    centred = pos.copy(order="F")
+    oracle.center_particles(centred, opar)
+    ctx = gpu.Context(0)
+    try:
+        p_in = pos.copy(order="F")
+        args = [hsml, m, rho, q, rho]
+        if on_device:
+            dev = torch.device("cuda", 0)
+            p_in = torch.from_numpy(np.ascontiguousarray(pos.T)).to(dev).T
+            args = [torch.from_numpy(a).to(dev) for a in args]
+        img, st = gpu.sphMapping(p_in, *args, param=gpu.mappingParameters(**kw),
+                                 kernel=gpu.Cubic(2), precision="fp32c", deterministic=det,
+                                 show_progress=False, return_stats=True, context=ctx)
+    finally:
+        ctx.close()
+    assert st["n_reruns"] >= 1
+    assert st["deposits"] == info["deposits"]
+    img = img.cpu().numpy() if hasattr(img, "cpu") else img
+    assert rel_linf(img, ref, 1e-9) <= 1e-5
+    got_pos = p_in.cpu().numpy() if hasattr(p_in, "cpu") else p_in
+    assert np.array_equal(got_pos, centred)
