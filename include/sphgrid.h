@@ -193,6 +193,26 @@ typedef struct sphg_grads {
 int sphg_map(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
              const sphg_particles *parts, double *out, void *stream, sphg_stats *stats);
 
+/* map_it's projection (cic_interpolation.jl:314-345, rotate_particles.jl,
+ * rotate_parameters.jl): the positions are read through it while mapping, and
+ * the caller's arrays are left intact, as map_it maps a copy.
+ * SPHG_PROJ_XZ / _YZ permute the axes (rotate_to_xz_plane! / _yz_plane!:
+ * (x, z, y) and (y, z, x)) and the parameters with them (center and limits
+ * permuted, Npixels = max(Npixels), the same boxsize).  SPHG_PROJ_MATRIX
+ * applies the row-major 3 x 3 `matrix` in FP64 -- rotate_3D's RotXYZ(a, b, c)
+ * = Rx(a) Ry(b) Rz(c) -- with the parameters unchanged, and maps the rotated
+ * positions as Float64 (Julia promotes them).  SPHG_CENTER_INPLACE is taken
+ * as SPHG_CENTER_READONLY. */
+enum { SPHG_PROJ_XY = 0, SPHG_PROJ_XZ = 1, SPHG_PROJ_YZ = 2, SPHG_PROJ_MATRIX = 3 };
+typedef struct sphg_projection {
+  int32_t kind;
+  int32_t reserved; /* 0 */
+  double matrix[9];
+} sphg_projection;
+int sphg_map_projected(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
+                       const sphg_particles *parts, const sphg_projection *proj, double *out,
+                       void *stream, sphg_stats *stats);
+
 /* reduce_image_2D / reduce_image_3D (reduce_image.jl:8-55) of a raw
  * (P^D, Nq+1) accumulator into the output layout of `opt` (device memory). */
 int sphg_reduce(sphg_context *ctx, const sphg_params *par, const sphg_options *opt, int32_t n_q,

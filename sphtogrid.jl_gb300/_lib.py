@@ -30,6 +30,7 @@ SPHG_F32, SPHG_F64 = 0, 1
 PREC = {"fp64": 0, "fp32c": 1}
 CENTER_NONE, CENTER_INPLACE, CENTER_READONLY = 0, 1, 2
 MEM_DEVICE, MEM_HOST = 0, 1
+PROJ_XY, PROJ_XZ, PROJ_YZ, PROJ_MATRIX = 0, 1, 2, 3
 
 
 class SphgParams(C.Structure):
@@ -87,6 +88,10 @@ class SphgOptions(C.Structure):
         ("raw_accumulator", C.c_int32),
         ("reserved", C.c_int32 * 3),
     ]
+
+
+class SphgProjection(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("matrix", C.c_double * 9)]
 
 
 class SphgStats(C.Structure):
@@ -172,6 +177,10 @@ def lib():
         L.sphg_adjoint.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
                                    C.POINTER(SphgParticles), vp, vp, C.POINTER(SphgGrads), vp]
         L.sphg_adjoint.restype = i32
+        L.sphg_map_projected.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
+                                         C.POINTER(SphgParticles), C.POINTER(SphgProjection), vp,
+                                         vp, C.POINTER(SphgStats)]
+        L.sphg_map_projected.restype = i32
         L.sphg_probe_smem_rate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.sphg_probe_smem_rate.restype = i32
         L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]

@@ -261,8 +261,11 @@ int64_t sphg_output_len(const sphg_params* par, const sphg_options* opt, int32_t
   return -1;
 }
 
-int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
-             double* out, void* stream, sphg_stats* stats) {
+namespace {
+// sphg_map with an optional position transform (xform: 0 none, 1 axis
+// permutation `perm`, 2 FP64 matrix `rot`; see sphg::DevParticles).
+int map_impl(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
+             int xform, const int* perm, const double* rot, double* out, void* stream, sphg_stats* stats) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!par || !opt || !pt || !out) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
@@ -377,6 +380,9 @@ again:
   d.nq = nq;
   d.qsp = pt->q_stride_p;
   d.qsk = pt->q_stride_k;
+  d.xform = xform;
+  for (int k = 0; k < 3; ++k) d.perm[k] = perm ? perm[k] : k;
+  for (int k = 0; k < 9; ++k) d.rot[k] = rot ? rot[k] : 0.0;
   double* dout = out;
   if (host) {
     d.pos = ws + o_pos;
@@ -543,6 +549,44 @@ again:
   if (hs.flags & sphg::kFlagTimeout) return fail(ctx, SPHG_ERR_TIMEOUT, "");
   ctx->last_error.clear();
   return SPHG_OK;
+}
+}  // namespace
+
+int sphg_map(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
+             double* out, void* stream, sphg_stats* stats) {
+  return map_impl(ctx, par, opt, pt, 0, nullptr, nullptr, out, stream, stats);
+}
+
+int sphg_map_projected(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
+                       const sphg_particles* pt, const sphg_projection* proj, double* out, void* stream,
+                       sphg_stats* stats) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  if (!par || !opt || !proj) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
+  if (proj->reserved) return fail(ctx, SPHG_ERR_ARG, "reserved projection field must be 0");
+  sphg_options o = *opt;  // map_it maps a copy: the caller's positions stay as they are
+  if (o.center == SPHG_CENTER_INPLACE) o.center = SPHG_CENTER_READONLY;
+  if (proj->kind == SPHG_PROJ_XY) return map_impl(ctx, par, &o, pt, 0, nullptr, nullptr, out, stream, stats);
+  if (proj->kind == SPHG_PROJ_MATRIX) {
+    for (int k = 0; k < 9; ++k)
+      if (!std::isfinite(proj->matrix[k])) return fail(ctx, SPHG_ERR_ARG, "projection matrix not finite");
+    return map_impl(ctx, par, &o, pt, 2, nullptr, proj->matrix, out, stream, stats);
+  }
+  if (proj->kind != SPHG_PROJ_XZ && proj->kind != SPHG_PROJ_YZ) return fail(ctx, SPHG_ERR_ARG, "projection kind");
+  // rotate_to_xz_plane / rotate_to_yz_plane of the parameters
+  // (rotate_parameters.jl:6-40): permuted centre and limits, the largest
+  // Npixels, the same boxsize
+  const int xz = proj->kind == SPHG_PROJ_XZ;
+  const int perm[3] = {xz ? 0 : 1, 2, xz ? 1 : 0};
+  const double* lims[3] = {par->x_lim, par->y_lim, par->z_lim};
+  const double cen[3] = {par->center[perm[0]], par->center[perm[1]], par->center[perm[2]]};
+  int64_t npix = par->Npixels[0];
+  for (int k = 1; k < 3; ++k) npix = par->Npixels[k] > npix ? par->Npixels[k] : npix;
+  sphg_params rp;
+  const double m1 = -1.0;
+  if (int st = sphg_mapping_parameters(lims[perm[0]], lims[perm[1]], lims[perm[2]], cen, m1, m1, m1, m1, npix,
+                                       par->boxsize, &rp))
+    return fail(ctx, st, "rotated parameters");
+  return map_impl(ctx, &rp, &o, pt, 1, perm, nullptr, out, stream, stats);
 }
 
 int sphg_reduce(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, int32_t n_q,

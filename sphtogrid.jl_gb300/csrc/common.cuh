@@ -69,6 +69,13 @@ struct DevParticles {
   const void *hsml, *mass, *rho, *w, *q;
   int nq;
   int64_t qsp, qsk;
+  // map_it's projection (cic_interpolation.jl:330-345), read through on the
+  // fly: 0 none; 1 axis permutation (coordinate d is input component
+  // perm[d], exact, input precision); 2 FP64 3x3 matrix (row-major; the
+  // rotated positions are Float64, as Julia promotes them)
+  int xform = 0;
+  int perm[3] = {0, 1, 2};
+  double rot[9] = {};
 };
 
 // Mapping parameters the kernels need (derived on the host).
@@ -148,15 +155,24 @@ __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const 
                                                   bool store_pos, PrepFP64* o) {
   double c[3];
   bool in = true;
+  double xr[3] = {0.0, 0.0, 0.0};
+  if (pt.xform == 2) {  // (R0 x0 + R1 x1) + R2 x2 per row, in FP64
+    const double x0 = ld_elem(pt.pos_dtype, pt.pos, p * pt.sp);
+    const double x1 = ld_elem(pt.pos_dtype, pt.pos, p * pt.sp + pt.sc);
+    const double x2 = ld_elem(pt.pos_dtype, pt.pos, p * pt.sp + 2 * pt.sc);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xr[d] = (pt.rot[3 * d] * x0 + pt.rot[3 * d + 1] * x1) + pt.rot[3 * d + 2] * x2;
+  }
+  const int vdt = pt.xform == 2 ? 1 : pt.pos_dtype;  // precision the centring rounds to
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int64_t off = p * pt.sp + d * pt.sc;
-    double v = ld_elem(pt.pos_dtype, pt.pos, off);
+    const int64_t off = p * pt.sp + (pt.xform == 1 ? pt.perm[d] : d) * pt.sc;
+    double v = pt.xform == 2 ? xr[d] : ld_elem(pt.pos_dtype, pt.pos, off);
     if (mp.center_mode != 0) {
-      v = round_to(pt.pos_dtype, v - mp.cen[d]);
+      v = round_to(vdt, v - mp.cen[d]);
       if (mp.periodic && fabs(v) > mp.boxsize / 2)
-        v = round_to(pt.pos_dtype, v > 0 ? v - mp.boxsize / 2 : v + mp.boxsize / 2);
-      if (mp.center_mode == 1 && store_pos) st_elem(pt.pos_dtype, pt.pos, off, v);
+        v = round_to(vdt, v > 0 ? v - mp.boxsize / 2 : v + mp.boxsize / 2);
+      if (mp.center_mode == 1 && store_pos && pt.xform == 0) st_elem(pt.pos_dtype, pt.pos, off, v);
     }
     c[d] = v;
     if (mp.filter && !(mp.lo[d] <= v && v <= mp.hi[d])) in = false;

@@ -17,6 +17,7 @@ module SPHtoGridGB300
 
 using SPHtoGrid: mappingParameters
 using SPHKernels: AbstractSPHKernel, Cubic, Quintic, WendlandC4, WendlandC6, WendlandC8
+using Rotations: RotXYZ  # a dependency of the reference (rotate_particles.jl)
 
 const libsphgrid = get(ENV, "SPHGRID_LIB", joinpath(@__DIR__, "..", "libsphgrid.so"))
 
@@ -160,6 +161,59 @@ function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
     end
     pos === Pos || (Pos .= pos)  # the reference centres the caller's array in place
     show_progress && @info "Particles in image: $(st.n_mapped) / $N, deposits: $(st.deposits)"
+    return out
+end
+
+# ------------------------------------------------------------------ map_it
+
+struct SphgProjection
+    kind::Int32          # 0 xy, 1 xz, 2 yz, 3 matrix
+    reserved::Int32
+    matrix::NTuple{9,Float64}  # row-major
+end
+
+"""
+    map_it(pos_in, hsml, mass, rho, bin_q, weights=rho; param, kernel=WendlandC6(2),
+           projection="xy", reduce_image=true, calc_mean=true, precision=:fp64)
+
+The map of `map_it` (cic_interpolation.jl:314-380) on the GPU: the positions
+are read through the projection ("xy", "xz", "yz" or three Euler angles in
+degrees, RotXYZ as rotate_3D builds it) and `pos_in` is left intact.  Returns
+the map; write it with the reference's `write_fits_image` as map_it does.
+"""
+function map_it(pos_in::Array{<:Real}, hsml, mass, rho, bin_q, weights=rho;
+                param::mappingParameters, kernel::AbstractSPHKernel=WendlandC6(2),
+                projection="xy", reduce_image::Bool=true, calc_mean::Bool=true,
+                precision::Symbol=:fp64)
+    T = (eltype(hsml) == Float32 && eltype(mass) == Float32 && eltype(rho) == Float32 &&
+         eltype(bin_q) == Float32 && eltype(weights) == Float32) ? Float32 : Float64
+    pos = eltype(pos_in) <: Union{Float32,Float64} ? pos_in : Float64.(pos_in)
+    h, m, r, w, q = T.(hsml), T.(mass), T.(rho), T.(weights), T.(bin_q)
+    N = length(m)
+    nq = ndims(q) == 1 ? 1 : size(q, 1)
+    P = param.Npixels[1]
+    out = zeros(Float64, P, P, nq)
+    zero9 = ntuple(_ -> 0.0, 9)
+    proj = projection == "xy" ? SphgProjection(0, 0, zero9) :
+           projection == "xz" ? SphgProjection(1, 0, zero9) :
+           projection == "yz" ? SphgProjection(2, 0, zero9) :
+           SphgProjection(3, 0, Tuple(vec(permutedims(Matrix(RotXYZ(deg2rad.(projection)...))))))
+    GC.@preserve pos h m r w q out begin
+        pt = SphgParticles(N, dtype_id(eltype(pos)), dtype_id(T), pointer(pos), 3, 1,
+                           pointer(h), pointer(m), pointer(r), pointer(w), pointer(q),
+                           Int32(nq), Int32(0), ndims(q) == 1 ? 1 : nq, ndims(q) == 1 ? 0 : 1)
+        kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
+        # centre mode 2: read-only (map_it maps a copy of the positions)
+        opt = SphgOptions(2, kernel_id(kernel), kdim, reduce_image, false, calc_mean,
+                          precision === :fp32c ? 1 : 0, 0, 2, 1, 1, 0, 0, (0, 0, 0))
+        st = SphgStats()
+        status = ccall((:sphg_map_projected, libsphgrid), Cint,
+                       (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles},
+                        Ref{SphgProjection}, Ptr{Float64}, Ptr{Cvoid}, Ref{SphgStats}),
+                       context(), SphgParams(param), opt, pt, proj, pointer(out), C_NULL, st)
+        status == 0 || error(unsafe_string(ccall((:sphg_last_error, libsphgrid), Cstring,
+                                                 (Ptr{Cvoid},), context())))
+    end
     return out
 end
 

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes as C
 import logging
+import math
 import time
 
 import numpy as np
@@ -128,7 +129,7 @@ def sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, RM=None, *, param: Ma
 
 def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
                dims, calc_mean, sort_z, precision, deterministic, device, center_in_place=True,
-               context=None):
+               context=None, projection=None):
     if not isinstance(Pos, np.ndarray) or Pos.ndim != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) array")
     n = Pos.shape[1]
@@ -198,8 +199,13 @@ def _map_numpy(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
         pt.q_stride_p, pt.q_stride_k = q.strides[1] // q.itemsize, q.strides[0] // q.itemsize
     st = _lib.SphgStats()
     ctx = context if context is not None else _lib.default_context(device)
-    _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
-                                   flat.ctypes.data, None, C.byref(st)), ctx.handle)
+    if projection is None:
+        _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
+                                       flat.ctypes.data, None, C.byref(st)), ctx.handle)
+    else:
+        _lib.check(_lib.lib().sphg_map_projected(ctx.handle, C.byref(param._c), C.byref(opts),
+                                                 C.byref(pt), C.byref(projection), flat.ctypes.data,
+                                                 None, C.byref(st)), ctx.handle)
     if writeback is not None:
         writeback[...] = pos
     return _shape_out(flat, P, nq, dims, return_both_maps and dims == 2), _stats_dict(st)
@@ -222,7 +228,8 @@ def _torch_dt(t):
     raise TypeError(f"unsupported dtype {t.dtype}")
 
 def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_image, return_both_maps,
-               dims, calc_mean, sort_z, precision, deterministic, center_in_place=True, context=None):
+               dims, calc_mean, sort_z, precision, deterministic, center_in_place=True, context=None,
+               projection=None):
     import torch
     if Pos.dim() != 2 or Pos.shape[0] != 3:
         raise ValueError("Pos must be a (3, N) tensor")
@@ -262,7 +269,86 @@ def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
     st = _lib.SphgStats()
     ctx = context if context is not None else _lib.default_context(dev.index if dev.index is not None else 0)
     stream = _lib.stream_handle(torch.cuda.current_stream(dev))
-    _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
-                                   C.c_void_p(flat.data_ptr()), stream, C.byref(st)),
-               ctx.handle)
+    if projection is None:
+        _lib.check(_lib.lib().sphg_map(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
+                                       C.c_void_p(flat.data_ptr()), stream, C.byref(st)),
+                   ctx.handle)
+    else:
+        _lib.check(_lib.lib().sphg_map_projected(ctx.handle, C.byref(param._c), C.byref(opts),
+                                                 C.byref(pt), C.byref(projection),
+                                                 C.c_void_p(flat.data_ptr()), stream, C.byref(st)),
+                   ctx.handle)
     return _shape_out(flat, P, nq, dims, return_both_maps and dims == 2), _stats_dict(st)
+
+
+def rotation_matrix_xyz(alpha: float, beta: float, gamma: float) -> np.ndarray:
+    """RotXYZ(alpha, beta, gamma) = Rx(alpha) Ry(beta) Rz(gamma), angles in
+    degrees, as rotate_3D builds it (rotate_particles.jl:7-14); row-major."""
+    a, b, c = (math.radians(float(x)) for x in (alpha, beta, gamma))
+    sa, ca, sb, cb, sc, cc = math.sin(a), math.cos(a), math.sin(b), math.cos(b), math.sin(c), math.cos(c)
+    return np.array([[cb * cc, -(cb * sc), sb],
+                     [ca * sc + sa * sb * cc, ca * cc - sa * sb * sc, -(sa * cb)],
+                     [sa * sc - ca * sb * cc, sa * cc + ca * sb * sc, ca * cb]], dtype=np.float64)
+
+
+def _projection(projection):
+    pr = _lib.SphgProjection()
+    if isinstance(projection, str):
+        kinds = {"xy": _lib.PROJ_XY, "xz": _lib.PROJ_XZ, "yz": _lib.PROJ_YZ}
+        if projection not in kinds:
+            raise ValueError("projection must be either along in 'xy', 'xz', or 'yz' plane of "
+                             "defined by a vector of Euler angles!")
+        pr.kind = kinds[projection]
+        return pr, projection
+    angles = [float(x) for x in projection]
+    if len(angles) != 3:
+        raise ValueError("projection must be either along in 'xy', 'xz', or 'yz' plane of "
+                         "defined by a vector of Euler angles!")
+    pr.kind = _lib.PROJ_MATRIX
+    for k, v in enumerate(rotation_matrix_xyz(*angles).reshape(-1)):
+        pr.matrix[k] = v
+    name = "alpha=%0.2fbeta=%0.2fgamma=%0.2f" % tuple(angles)
+    return pr, name
+
+
+def map_it(pos_in, hsml, mass, rho, bin_q, weights, RM=None, *, param: MappingParameters,
+           kernel: SPHKernel | None = None, snap: int = 0, units: str = "",
+           image_prefix: str = "dummy", reduce_image: bool = True, parallel: bool = True,
+           calc_mean: bool = True, show_progress: bool = True, sort_z: bool = False,
+           stokes: bool = False, renorm: bool = False, projection="xy", precision: str = "fp64",
+           deterministic: bool = False, device: int = 0, write_fits: bool = True):
+    """map_it (cic_interpolation.jl:314-380): map the particles seen along a
+    projection ('xy', 'xz', 'yz' or three Euler angles in degrees) and write
+    ``<image_prefix>.<projection>.fits`` with the caller's parameters.
+
+    The projection is applied while the positions are read (K1), so
+    ``pos_in`` is left intact as the reference's copy leaves it.  Defaults
+    are the reference's (``calc_mean=True``, WendlandC6 in 2D).  Returns the
+    map (the reference returns nothing)."""
+    from .parameters import WendlandC6
+    if RM is not None or stokes:
+        raise NotImplementedError(
+            "Faraday rotation / Stokes mapping (cic_shared.jl:129-159) is not supported")
+    if sort_z:
+        raise NotImplementedError("sort_z of projected positions is not supported")
+    kernel = kernel if kernel is not None else WendlandC6(2)
+    pr, name = _projection(projection)
+    if weights is None:
+        weights = rho
+    t0 = time.perf_counter()
+    if _is_torch_cuda(pos_in):
+        image, stats = _map_torch(pos_in, hsml, mass, rho, bin_q, weights, param, kernel, reduce_image,
+                                  False, 2, calc_mean, False, precision, deterministic, False, None, pr)
+    else:
+        image, stats = _map_numpy(pos_in, hsml, mass, rho, bin_q, weights, param, kernel, reduce_image,
+                                  False, 2, calc_mean, False, precision, deterministic, device, False,
+                                  None, pr)
+    if renorm:
+        image = image / image.max()
+    if show_progress:
+        log.info("map_it %s: %d / %d particles mapped, %d deposits, %.3f s", name, stats["n_mapped"],
+                 stats["n_in"], stats["deposits"], time.perf_counter() - t0)
+    if write_fits:
+        from .io import write_fits_image
+        write_fits_image(f"{image_prefix}.{name}.fits", image, param, snap=snap, units=units)
+    return image
