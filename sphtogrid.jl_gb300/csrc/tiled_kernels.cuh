@@ -245,7 +245,7 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
   for (int f = lane; f < F; f += 32) {
     const int a = fdiv(f, inv_njk);
     const int rr = f - a * njk;
-    const int b = fdiv(rr, inv_nz), c = rr - b * dm.z;
+    const int b = DIMS == 3 ? fdiv(rr, inv_nz) : rr, c = DIMS == 3 ? rr - b * dm.z : 0;
     const float2 ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
     cell_term<DIMS, KERN>(kern, tab[0][a], tab[1][b], ez, hinv, s, comp, umin);
   }
@@ -447,10 +447,19 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
       const int64_t F = (int64_t)dm.x * dm.y * dm.z;
       if (F > A.large_cells) continue;  // two-phase path (k_large_partials)
       float s = 0.0f, comp = 0.0f, umin = 3.0e38f;
-      if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab)
-        record_sum_tab<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, lane, tab, plane, s, comp, umin);
-      else
+      if (dm.x <= kNormTab && dm.y <= kNormTab && dm.z <= kNormTab) {
+        const float4 g = A.geo[g0 + j];
+        // a run-time kernel shape is dispatched once per record, so the
+        // cell loop evaluates a compile-time shape
+        if (KERN >= 0) record_sum_tab<DIMS, KERN>(A.kern, g, dm, lane, tab, plane, s, comp, umin);
+        else if (A.kern == 0) record_sum_tab<DIMS, 0>(0, g, dm, lane, tab, plane, s, comp, umin);
+        else if (A.kern == 1) record_sum_tab<DIMS, 1>(1, g, dm, lane, tab, plane, s, comp, umin);
+        else if (A.kern == 2) record_sum_tab<DIMS, 2>(2, g, dm, lane, tab, plane, s, comp, umin);
+        else if (A.kern == 3) record_sum_tab<DIMS, 3>(3, g, dm, lane, tab, plane, s, comp, umin);
+        else record_sum_tab<DIMS, 4>(4, g, dm, lane, tab, plane, s, comp, umin);
+      } else {
         record_sum_fp32<DIMS, KERN>(A.kern, A.geo[g0 + j], dm, 0, F, lane, 32, s, comp, umin);
+      }
       warp_reduce_comp(s, comp, umin);
       if (lane == j) {
         my_s = s;
@@ -692,6 +701,34 @@ __device__ __forceinline__ void prepare_pair(const TiledArgs& A, int r, int ox, 
     for (int k = 0; k < NQ; ++k) H.cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
 }
 
+// The cells of one (record, tile) pair: the intersection's n = na nb nc
+// cells, lane-strided, from the per-axis tables.  KERN is a compile-time
+// shape here.
+template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
+__device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
+                                              float cw, const float* cq, int nq, int TV, float* hi, float* lo,
+                                              unsigned long long* fx, int lane) {
+  const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
+  for (int e = lane; e < n; e += 32) {
+    const int bc = DIMS == 3 ? fdiv(e, inv_nc) : e;  // 2D: nc == 1
+    const int c = DIMS == 3 ? e - bc * nc : 0;
+    const int a = fdiv(bc, inv_nb);
+    const int b = bc - a * nb;
+    const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
+    const float u = u_of((ex.x + ey.x) + ez.x, hinv);
+    if (u <= 1.0f) {
+      const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
+      const int li = lbase + (a * TY + b) * TZ + c;
+      acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+#pragma unroll
+      for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+        if (NQ == 0 && k >= nq) break;
+        acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
+      }
+    }
+  }
+}
+
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh) {
   constexpr int TV = TX * TY * TZ;
@@ -798,26 +835,17 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
                                               : axis_sq(ax == 0 ? H.fx : (ax == 1 ? H.fy : H.fz), h, c);
         }
         __syncwarp();
-        const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
-        const int lbase = H.lbase;
-        for (int e = lane; e < n; e += 32) {
-          const int bc = fdiv(e, inv_nc);
-          const int c = e - bc * nc;
-          const int a = fdiv(bc, inv_nb);
-          const int b = bc - a * nb;
-          const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
-          const float u = u_of((ex.x + ey.x) + ez.x, hinv);
-          if (u <= 1.0f) {
-            const float gw = shape_f<KERN>(A.kern, u) * (ex.y * ey.y * ez.y);
-            const int li = lbase + (a * TY + b) * TZ + c;
-            acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
-#pragma unroll
-            for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
-              if (NQ == 0 && k >= nq) break;
-              acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
-            }
-          }
-        }
+        // a run-time kernel shape is dispatched once per pair, so the cell
+        // loop evaluates a compile-time shape
+#define SPHG_CELLS(K) \
+  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, H.lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
+        if (KERN >= 0) SPHG_CELLS(KERN >= 0 ? KERN : 0);
+        else if (A.kern == 0) SPHG_CELLS(0);
+        else if (A.kern == 1) SPHG_CELLS(1);
+        else if (A.kern == 2) SPHG_CELLS(2);
+        else if (A.kern == 3) SPHG_CELLS(3);
+        else SPHG_CELLS(4);
+#undef SPHG_CELLS
       }
       __syncwarp();  // the tables are refilled for the next pair
     }

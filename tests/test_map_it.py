@@ -93,4 +93,7 @@ def test_map_it_matches_oracle(gpu, oracle, tmp_path, projection, dtype, precisi
     from sphtogrid_gb300 import io
     got, fpar, _, _ = io.read_fits_image(fits)
     assert np.array_equal(got, np.asarray(img)[:, :, 0])
-    assert fpar.center == par.center  # written with the caller's parameters
+    # written with the caller's parameters; read_fits_image rebuilds them from
+    # the limits (io.jl:132-138), so the centre comes back as their midpoint
+    assert fpar.x_lim == par.x_lim and fpar.y_lim == par.y_lim and fpar.z_lim == par.z_lim
+    assert np.allclose(fpar.center, par.center, rtol=0, atol=1e-15)
