@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(1024) kb_scan(BatchDev B) {
   scan_tiles(B.maps[blockIdx.x], part);
 }
 
-__global__ void __launch_bounds__(256) kb_norm(BatchDev B) {
+__global__ void __launch_bounds__(256, 4) kb_norm(BatchDev B) {
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int m = 0; m < B.n_maps; ++m) {

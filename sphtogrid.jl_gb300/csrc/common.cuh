@@ -128,6 +128,19 @@ __device__ __forceinline__ bool floor_int(double v, int64_t* out) {
   return true;
 }
 
+// 1/x to FP32 accuracy (relative error below 2^-22) over the whole FP64
+// range, without an FP64 division: the mantissa's reciprocal in FP32, the
+// exponent negated by bit arithmetic.  Zero, subnormal and non-finite x take
+// the FP64 division.
+__device__ __forceinline__ double rcp_approx(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0 || ex >= 0x7fe || ex <= 1) return 1.0 / x;
+  const double m = __longlong_as_double((b & 0x800fffffffffffffLL) | (1023LL << 52));  // +-[1, 2)
+  const double r = (double)__frcp_rn((float)m);                                        // +-(0.5, 1]
+  return r * __longlong_as_double((long long)(2046 - ex) << 52);                       // * 2^(1023 - ex)
+}
+
 // Julia min/max on finite floats.
 __device__ __forceinline__ double jmin(double a, double b) { return b < a ? b : a; }
 __device__ __forceinline__ double jmax(double a, double b) { return b > a ? b : a; }
@@ -150,7 +163,10 @@ enum { kPrepSkip = 0, kPrepMapped = 1, kPrepNonFinite = 2 };
 // (cic_2D.jl:154-168), get_quantities_2D/3D (cic_2D.jl:80-91,
 // cic_3D.jl:87-97), get_xyz and pix_index_min_max (cic_shared.jl:46-99).
 // `store_pos` writes the centred position back (SPHG_CENTER_INPLACE).
-template <int DIMS>
+// FACTORS = false skips the per-particle factors (h_inv, area, col, vol,
+// knorm: FP64 divisions) for callers that derive their own; the centring,
+// filter and pixel ranges are the same either way.
+template <int DIMS, bool FACTORS = true>
 __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const DevMapParams& mp, int64_t p,
                                                   bool store_pos, PrepFP64* o) {
   double c[3];
@@ -190,18 +206,21 @@ __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const 
   o->wgt = ld_elem(pt.attr_dtype, pt.w, p);
   const double hsml = ld_elem(pt.attr_dtype, pt.hsml, p) * L;
   o->hsml = hsml;
-  o->h_inv = 1.0 / hsml;
+  o->h_inv = o->knorm = 0.0;
   o->area = o->col = o->vol = 0.0;
-  if (DIMS == 2) {
-    o->area = (2.0 * hsml) * (2.0 * hsml);
-    const double rho = o->rho_in * (1.0 / (L * L * L));
-    o->col = o->m_in / rho / o->area;
-  } else {
-    const double rho = o->rho_in / (L * L * L);
-    o->vol = o->m_in / rho;
+  if (FACTORS) {
+    o->h_inv = 1.0 / hsml;
+    if (DIMS == 2) {
+      o->area = (2.0 * hsml) * (2.0 * hsml);
+      const double rho = o->rho_in * (1.0 / (L * L * L));
+      o->col = o->m_in / rho / o->area;
+    } else {
+      const double rho = o->rho_in / (L * L * L);
+      o->vol = o->m_in / rho;
+    }
+    const double hd = mp.kernel_dim == 2 ? o->h_inv * o->h_inv : o->h_inv * o->h_inv * o->h_inv;
+    o->knorm = mp.sigma * hd;
   }
-  const double hd = mp.kernel_dim == 2 ? o->h_inv * o->h_inv : o->h_inv * o->h_inv * o->h_inv;
-  o->knorm = mp.sigma * hd;
   double x = c[0] * L, y = c[1] * L, z = c[2] * L;
   x += 0.5 * (double)P;
   y += 0.5 * (double)P;

@@ -26,7 +26,7 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
     const int64_t p = base + threadIdx.x;
     PrepFP64 q;
     int state = kPrepSkip;
-    if (p < A.pt.n) state = prep_particle_fp64<DIMS>(A.pt, A.mp, p, true, &q);
+    if (p < A.pt.n) state = prep_particle_fp64<DIMS, false>(A.pt, A.mp, p, true, &q);
     if (state == kPrepNonFinite) flags |= kFlagNonFinite;
     int ni = 0, nj = 0, nk = 0;
     if (state == kPrepMapped) {
@@ -54,12 +54,21 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
       A.geo[r] = make_float4(__double2float_rn(q.x - (double)i0), __double2float_rn(q.y - (double)j0),
                              DIMS == 3 ? __double2float_rn(q.z - (double)k0) : 0.0f,
                              __double2float_rn(q.hsml));
-      // weight factor numerator: area*w*dz (cic_2D.jl:187-188) / vol*w*L (cic_3D.jl:168-169)
-      A.cp[r] = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
-      A.aux[r] = q.rho_in * q.knorm / (A.mp.L * A.mp.L * A.mp.L);
+      // weight factor numerator, area*w*dz (cic_2D.jl:187-188) = w m / rho_pix
+      // or vol*w*L (cic_3D.jl:168-169) = w m L / rho_pix, with
+      // rho_pix = rho / L^3; FP32 accuracy suffices here (the FP32 method
+      // derives FP32 factors from it; ill-conditioned records redo it in
+      // FP64), so no FP64 division
+      const double L = A.mp.L, L3 = L * L * L;
+      const double wm_rho = q.wgt * q.m_in * L3 * rcp_approx(q.rho_in);
+      A.cp[r] = DIMS == 2 ? wm_rho : wm_rho * L;
+      // 3D mass diagnostic factor rho/L^3 * kernel normalisation
+      const double hi_ = rcp_approx(q.hsml);
+      A.aux[r] = q.rho_in * (A.mp.sigma * (A.mp.kernel_dim == 2 ? hi_ * hi_ : hi_ * hi_ * hi_)) * rcp_approx(L3);
       for (int k = 0; k < A.pt.nq; ++k)
         A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
-            : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
+            : A.pt.attr_dtype == 0 ? __ldg((const float*)A.pt.q + p * A.pt.qsp + k * A.pt.qsk)
+                                   : __double2float_rn(ld_elem(A.pt.attr_dtype, A.pt.q, p * A.pt.qsp + k * A.pt.qsk));
       if ((int64_t)ni * nj * nk > A.large_cells) A.large[atomicAdd(A.n_large, 1)] = r;
       // (particle, tile) overlaps
       const int tx0 = i0 / A.tdim[0], tx1 = (i0 + ni - 1) / A.tdim[0];
