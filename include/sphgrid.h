@@ -213,6 +213,26 @@ int sphg_map_projected(sphg_context *ctx, const sphg_params *par, const sphg_opt
                        const sphg_particles *parts, const sphg_projection *proj, double *out,
                        void *stream, sphg_stats *stats);
 
+/* healpix_map's particle loop (healpix_interpolation/main.jl:129-204) on
+ * the GPU in FP64: the particles as filter_sort_particles leaves them
+ * (centred on the observer and selected; their order does not matter),
+ * positions 3 per particle, device memory.  Skips particles with q == 0
+ * (unless calc_mean) and those closer than their hsml; adds into `allsky`
+ * and `weight` (12 nside^2 doubles each, RING ordering, zeroed by the
+ * caller).  stats: n_mapped, deposits (particle-pixel pairs), grid_mass and
+ * particle_mass as the reference accumulates them. */
+typedef struct sphg_healpix_params {
+  int64_t nside;     /* power of 2, 1 .. 8192 */
+  int32_t kernel;    /* SPHG_KERNEL_* */
+  int32_t kernel_dim;
+  int32_t calc_mean;
+  int32_t dtype;     /* SPHG_F32 / SPHG_F64 of all particle arrays */
+} sphg_healpix_params;
+int sphg_healpix_map(sphg_context *ctx, const sphg_healpix_params *hp, int64_t n, const void *pos,
+                     const void *hsml, const void *mass, const void *rho, const void *bin_q,
+                     const void *weights, double *allsky, double *weight, void *stream,
+                     sphg_stats *stats);
+
 /* reduce_image_2D / reduce_image_3D (reduce_image.jl:8-55) of a raw
  * (P^D, Nq+1) accumulator into the output layout of `opt` (device memory). */
 int sphg_reduce(sphg_context *ctx, const sphg_params *par, const sphg_options *opt, int32_t n_q,

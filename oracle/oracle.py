@@ -64,13 +64,17 @@ class OracleError(RuntimeError):
     pass
 
 
+HP_SRC_PATH = os.path.join(HERE, "healpix_oracle.c")
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (no FMA contraction, so the expression order
     of the reference is kept)."""
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC_PATH):
+    newest = max(os.path.getmtime(SRC_PATH), os.path.getmtime(HP_SRC_PATH))
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
         subprocess.check_call(
             ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-             "-o", LIB_PATH, SRC_PATH, "-lm", "-lpthread"])
+             "-o", LIB_PATH, SRC_PATH, HP_SRC_PATH, "-lm", "-lpthread"])
     return LIB_PATH
 
 
@@ -109,6 +113,16 @@ def lib():
                                            C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                            i64, vp, vp]
         L.orc_particle_contrib.restype = i64
+        L.hp_pix2vec_ring.argtypes = [i64, i64, dp]
+        L.hp_pix2vec_ring.restype = None
+        L.hp_ang2pix_ring.argtypes = [i64, C.c_double, C.c_double]
+        L.hp_ang2pix_ring.restype = i64
+        L.hp_vec2ang.argtypes = [C.c_double, C.c_double, C.c_double, dp, dp]
+        L.hp_vec2ang.restype = None
+        L.hp_query_disc_ring.argtypes = [i64, C.c_double, C.c_double, C.c_double, vp, i64]
+        L.hp_query_disc_ring.restype = i64
+        L.orc_healpix_map.argtypes = [i64, i32, i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp, dp, dp]
+        L.orc_healpix_map.restype = i64
         _lib = L
     return _lib
 
@@ -256,3 +270,69 @@ def sph_mapping(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param: OrcParams,
     else:
         image = out.reshape((P, P, P), order="F")
     return image, {"grid_mass": gm.value, "deposits": dep.value, "param": par}
+
+
+# ---------------------------------------------------------------- HEALPix
+
+def hp_pix2vec(nside: int, pix: int) -> np.ndarray:
+    v = (C.c_double * 3)()
+    lib().hp_pix2vec_ring(int(nside), int(pix), v)
+    return np.array(v[:])
+
+
+def hp_ang2pix(nside: int, theta: float, phi: float) -> int:
+    return int(lib().hp_ang2pix_ring(int(nside), float(theta), float(phi)))
+
+
+def hp_vec2ang(x: float, y: float, z: float):
+    t, p = C.c_double(), C.c_double()
+    lib().hp_vec2ang(float(x), float(y), float(z), C.byref(t), C.byref(p))
+    return t.value, p.value
+
+
+def hp_query_disc(nside: int, theta: float, phi: float, radius: float) -> np.ndarray:
+    cap = 1024
+    while True:
+        out = np.empty(cap, dtype=np.int64)
+        n = lib().hp_query_disc_ring(int(nside), float(theta), float(phi), float(radius), out.ctypes.data, cap)
+        if n <= cap:
+            return out[:n].copy()
+        cap = int(n)
+
+
+def filter_sort_particles(Pos, Hsml, M, Rho, Bin_q, Weights, center, radius_limits, calc_mean):
+    """filter_sort_particles (filter_particles.jl:19-53) with its selection as
+    written: the input-order shell mask `sel` picks entries of the descending
+    distance permutation, `sorted[sel]`.  Centres the caller's Pos in place."""
+    Pos -= np.asarray(center, dtype=Pos.dtype)[:, None]
+    dx = np.sqrt(Pos[0] ** 2 + Pos[1] ** 2 + Pos[2] ** 2)
+    sel = (radius_limits[0] <= dx) & (dx <= radius_limits[1])
+    if not calc_mean:
+        sel = sel[Bin_q[sel] > 0.0]  # raises unless the lengths agree, as the reference does
+    order = np.argsort(dx, kind="stable")[::-1]
+    idx = order[sel]
+    return (np.ascontiguousarray(Pos[:, idx].T), Hsml[idx], M[idx], Rho[idx], Bin_q[idx], Weights[idx])
+
+
+def healpix_map(Pos, Hsml, M, Rho, Bin_q, Weights, *, center=(0.0, 0.0, 0.0),
+                radius_limits=(0.0, np.inf), Nside=1024, kernel="cubic", kernel_dim=3, calc_mean=True):
+    """healpix_map (main.jl:92-227) in FP64 (the reference's path takes
+    Float64 inputs only: calculate_weights ties its Float64 weight arrays to
+    the position type).  Returns (allsky_map, weight_map, info)."""
+    npix = 12 * Nside * Nside
+    allsky = np.zeros(npix)
+    weight = np.zeros(npix)
+    if not calc_mean and np.sum(Bin_q) == 0:
+        return allsky, weight, {"mapped": 0}
+    pos, h, m, rho, q, w = filter_sort_particles(Pos, np.asarray(Hsml, np.float64),
+                                                 np.asarray(M, np.float64), np.asarray(Rho, np.float64),
+                                                 np.asarray(Bin_q, np.float64),
+                                                 np.asarray(Weights, np.float64), center,
+                                                 radius_limits, calc_mean)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pos, h, m, rho, q, w)]
+    gm, pm = C.c_double(), C.c_double()
+    mapped = lib().orc_healpix_map(int(Nside), KERNELS[kernel], int(kernel_dim), int(bool(calc_mean)),
+                                   arrs[1].shape[0], *[a.ctypes.data for a in arrs],
+                                   allsky.ctypes.data, weight.ctypes.data, C.byref(gm), C.byref(pm))
+    return allsky, weight, {"mapped": mapped, "grid_mass": gm.value, "particle_mass": pm.value,
+                            "selected": arrs[1].shape[0]}

@@ -17,6 +17,9 @@ def __getattr__(name):
     if name in ("sph_map_differentiable", "SPHMapFunction"):
         from . import autograd
         return getattr(autograd, name)
+    if name == "healpix_map":
+        from . import healpix
+        return healpix.healpix_map
     if name == "distributed_cic_map":
         from . import distributed
         return distributed.distributed_cic_map

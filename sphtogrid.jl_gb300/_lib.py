@@ -90,6 +90,11 @@ class SphgOptions(C.Structure):
     ]
 
 
+class SphgHealpixParams(C.Structure):
+    _fields_ = [("nside", C.c_int64), ("kernel", C.c_int32), ("kernel_dim", C.c_int32),
+                ("calc_mean", C.c_int32), ("dtype", C.c_int32)]
+
+
 class SphgProjection(C.Structure):
     _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("matrix", C.c_double * 9)]
 
@@ -181,6 +186,9 @@ def lib():
                                          C.POINTER(SphgParticles), C.POINTER(SphgProjection), vp,
                                          vp, C.POINTER(SphgStats)]
         L.sphg_map_projected.restype = i32
+        L.sphg_healpix_map.argtypes = [vp, C.POINTER(SphgHealpixParams), i64, vp, vp, vp, vp, vp, vp,
+                                       vp, vp, vp, C.POINTER(SphgStats)]
+        L.sphg_healpix_map.restype = i32
         L.sphg_probe_smem_rate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.sphg_probe_smem_rate.restype = i32
         L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]

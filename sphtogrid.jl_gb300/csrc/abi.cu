@@ -620,6 +620,42 @@ int sphg_accumulate(sphg_context* ctx, int64_t len, const double* part, double* 
   return SPHG_OK;
 }
 
+int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n, const void* pos,
+                     const void* hsml, const void* mass, const void* rho, const void* bin_q,
+                     const void* weights, double* allsky, double* weight, void* stream, sphg_stats* stats) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!hp || !allsky || !weight || n < 0) return fail(ctx, SPHG_ERR_ARG, "NULL argument or negative count");
+  if (n > 0 && (!pos || !hsml || !mass || !rho || !bin_q || !weights))
+    return fail(ctx, SPHG_ERR_ARG, "NULL particle array");
+  const int64_t ns = hp->nside;
+  if (ns < 1 || ns > 8192 || (ns & (ns - 1))) return fail(ctx, SPHG_ERR_ARG, "nside must be a power of 2 up to 8192");
+  if (hp->kernel < 0 || hp->kernel > 4 || (hp->kernel_dim != 2 && hp->kernel_dim != 3))
+    return fail(ctx, SPHG_ERR_ARG, "kernel");
+  if (!valid_dtype(hp->dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
+  if (n > 0)
+    sphg::launch_healpix(ns, hp->kernel, hp->kernel_dim, hp->calc_mean, hp->dtype, n, pos, hsml, mass, rho, bin_q,
+                         weights, allsky, weight, ctx->d_status, ctx->num_sms, s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const sphg::DevStatus hs = *ctx->h_status;
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->n_in = n;
+    stats->n_mapped = (int64_t)hs.n_mapped;
+    stats->deposits = (int64_t)hs.deposits;
+    stats->grid_mass = hs.grid_mass;
+    stats->particle_mass = hs.particle_mass;
+    stats->n_launches = n > 0 ? 1 : 0;
+  }
+  ctx->last_error.clear();
+  return SPHG_OK;
+}
+
 int sphg_probe_smem_rate(sphg_context* ctx, int kind, double* ops_per_s) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
   std::lock_guard<std::mutex> lk(ctx->mu);

@@ -20,6 +20,9 @@ cudaError_t probe_kernel_image(cudaFuncAttributes* fa);
 void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& mp, double* accq,
                        double* accw, int64_t PD, DevStatus* st, int num_sms, cudaStream_t s);
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s);
+void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtype, int64_t n, const void* pos,
+                    const void* hsml, const void* m, const void* rho, const void* q, const void* w,
+                    double* allsky, double* weight, DevStatus* st, int num_sms, cudaStream_t s);
 cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_per_s);
 void launch_accumulate(const double* part, double* sum, int64_t len, int num_sms, cudaStream_t s);
 void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one, double* out,
