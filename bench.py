@@ -126,7 +126,9 @@ def run_oracle(O, d, frac=1.0, threads=None):
     par = O.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["npix"])
     threads = threads or os.cpu_count()
     sl = slice(0, m)
-    pos = np.asfortranarray(d["pos"][:, sl])
+    # a fresh copy per call: the mapping centres its positions in place, as
+    # the reference's does (copied outside the timed region)
+    pos = np.array(d["pos"][:, sl], order="F", copy=True)
     t0 = time.perf_counter()
     img, info = O.sph_mapping(pos, d["hsml"][sl], d["mass"][sl], d["rho"][sl], d["bin_q"][sl],
                               d["weights"][sl], param=par, kernel=d["kernel"], dimensions=3,

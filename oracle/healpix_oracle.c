@@ -163,11 +163,12 @@ int64_t hp_query_disc_ring(int64_t nside, double theta, double phi, double radiu
     const double dphi = ysq <= 0.0 ? (x > 0.0 ? HP_PI : 0.0) : atan2(sqrt(ysq), x);
     if (dphi <= 0.0 && ysq <= 0.0 && x <= 0.0) continue;
     const double shift = sh ? 0.5 : 0.0;
-    int64_t lo = (int64_t)floor((double)nr / HP_TWOPI * (phi - dphi) - shift) + 1;
-    int64_t hi = (int64_t)floor((double)nr / HP_TWOPI * (phi + dphi) - shift);
-    if (hi - lo + 1 >= nr) {
-      lo = 0;
-      hi = nr - 1;
+    const double fa = floor((double)nr / HP_TWOPI * (phi - dphi) - shift);
+    const double fb = floor((double)nr / HP_TWOPI * (phi + dphi) - shift);
+    int64_t lo = 0, hi = nr - 1; /* a whole ring when the range spans it */
+    if (fb - fa < (double)nr) {
+      lo = (int64_t)fa + 1;
+      hi = (int64_t)fb;
     }
     for (int64_t k = lo; k <= hi; ++k) HP_PUSH(first + ((k % nr) + nr) % nr);
   }
@@ -214,6 +215,7 @@ int64_t orc_healpix_map(int64_t nside, int kernel, int kdim, int calc_mean, int6
     const double proj = asin(hsml[i] / dx);
     double theta, phi;
     hp_vec2ang(p[0], p[1], p[2], &theta, &phi);
+    if (!(isfinite(proj) && isfinite(theta) && isfinite(phi) && isfinite(q[i]))) continue;
     int64_t np = hp_query_disc_ring(nside, theta, phi, proj, idx, cap);
     while (np + 1 > cap) { /* grow the scratch and query again */
       cap = 2 * (np + 1);

@@ -643,6 +643,7 @@ int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n
   CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const sphg::DevStatus hs = *ctx->h_status;
+  if (hs.flags & sphg::kFlagNonFinite) return fail(ctx, SPHG_ERR_NONFINITE, "non-finite particle");
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->n_in = n;

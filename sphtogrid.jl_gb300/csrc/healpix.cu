@@ -156,14 +156,17 @@ __device__ __forceinline__ void hp_ring_range(const HpDisc& D, const HpRing& R, 
   const double x = (D.cosrad - R.z * D.z0) * D.xa, ysq = 1.0 - R.z * R.z - x * x;
   const double dphi = ysq <= 0.0 ? (x > 0.0 ? kPi : 0.0) : atan2(sqrt(ysq), x);
   const double shift = R.shifted ? 0.5 : 0.0;
-  int64_t l = (int64_t)floor((double)R.nr / kTwoPi * (D.phi - dphi) - shift) + 1;
-  int64_t h = (int64_t)floor((double)R.nr / kTwoPi * (D.phi + dphi) - shift);
-  if (h - l + 1 >= R.nr) {
-    l = 0;
-    h = R.nr - 1;
+  // the range in FP64 first: a whole ring when it spans the ring (or is
+  // not finite), so the integer range never exceeds the ring's pixels
+  const double fa = floor((double)R.nr / kTwoPi * (D.phi - dphi) - shift);
+  const double fb = floor((double)R.nr / kTwoPi * (D.phi + dphi) - shift);
+  if (!(fb - fa < (double)R.nr)) {
+    *lo = 0;
+    *hi = R.nr - 1;
+    return;
   }
-  *lo = l;
-  *hi = h;
+  *lo = (int64_t)fa + 1;
+  *hi = (int64_t)fb;
 }
 
 struct HpParticle {
@@ -230,6 +233,10 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
     double theta = atan2(sqrt(P.p[0] * P.p[0] + P.p[1] * P.p[1]), P.p[2]);
     double phi = atan2(P.p[1], P.p[0]);
     if (phi < 0.0) phi += kTwoPi;
+    if (!(isfinite(P.proj) && isfinite(theta) && isfinite(phi) && isfinite(P.q))) {
+      if (lane == 0) atomicOr(&H.st->flags, kFlagNonFinite);
+      continue;
+    }
     const HpDisc D = hp_disc(H.nside, theta, phi, P.proj);
     // the pixel holding the direction joins when the disc misses it
     const int64_t cpix = hp_ang2pix(H.nside, theta, phi);
