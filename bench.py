@@ -198,6 +198,12 @@ def bench_gpu(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload == "healpix":
+        import __graft_entry__ as graft
+        out = bench_healpix(graft.load_package(), dev, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     if args.workload == "large_hdr":
         import __graft_entry__ as graft
         out = bench_large(graft.load_package(), dev, args.steps, args.warmup)
@@ -543,6 +549,60 @@ def bench_large(pkg, dev, steps, warmup, n=2 ** 27, npix=4096, seed_grid=512):
             "pixels_carrying_weight": int(keep.sum())}
 
 
+HEALPIX_WORKLOAD = ("all-sky HEALPix map: N=2^20 particles in a shell 2 < r < 6 around the observer "
+                    "(directions isotropic), hsml uniform in [0.02, 0.8], m and rho uniform, Cubic, "
+                    "Nside=512, FP64, seed 0")
+
+
+def bench_healpix(pkg, dev, steps, warmup, n=2 ** 20, nside=512, cpu_sample=2 ** 12):
+    """The all-sky path: GPU healpix_map (FP64) against the oracle's restated
+    loop on one host core, on a bounded sample of the same particles."""
+    import torch
+    rng = np.random.default_rng(0)
+    r = rng.uniform(2.0, 6.0, n)
+    v = rng.standard_normal((3, n))
+    v /= np.linalg.norm(v, axis=0)
+    pos = np.asfortranarray(v * r)
+    hsml = rng.uniform(0.02, 0.8, n)
+    m = rng.uniform(0.5, 1.5, n)
+    rho = rng.uniform(0.5, 2.0, n)
+    q = rng.uniform(0.5, 2.0, n)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (hsml, m, rho, q, rho)]
+    tp = torch.from_numpy(np.ascontiguousarray(pos.T)).to(dev).T  # (3, N), xyz per particle
+
+    def once(k):
+        out = None
+        for _ in range(k):
+            p2 = tp.clone()
+            out = pkg.healpix_map(p2, *t, Nside=nside, kernel=pkg.Cubic(3), show_progress=False,
+                                  return_stats=True)
+        return out
+    once(warmup)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    _, _, st = once(steps)
+    torch.cuda.synchronize(dev)
+    gpu_s = (time.perf_counter() - t0) / steps
+    O = oracle_module()
+    m_s = min(cpu_sample, n)
+    t0 = time.perf_counter()
+    ra, rw, info = O.healpix_map(np.asfortranarray(pos[:, :m_s]).copy(order="F"), hsml[:m_s], m[:m_s],
+                                 rho[:m_s], q[:m_s], rho[:m_s], Nside=nside, kernel="cubic")
+    cpu_s = time.perf_counter() - t0
+    ga, gw, st_s = pkg.healpix_map(tp[:, :m_s].clone(), *[a[:m_s] for a in t], Nside=nside,
+                                   kernel=pkg.Cubic(3), show_progress=False, return_stats=True)
+    gw = gw.cpu().numpy()
+    sel = rw > 1e-9 * rw.max()
+    err = float((np.abs(gw[sel] - rw[sel]) / rw[sel]).max())
+    return {"workload": HEALPIX_WORKLOAD, "particles": n, "nside": nside,
+            "pixel_deposits": int(st["deposits"]), "gpu_s_per_map": gpu_s,
+            "gpu_pixel_deposits_per_s": st["deposits"] / gpu_s,
+            "cpu_baseline": {"kind": "port", "cores": 1, "sample": f"{m_s} of {n} particles",
+                             "pixel_deposits_per_s": st_s["deposits"] / cpu_s},
+            "speedup_vs_cpu_per_core": (st["deposits"] / gpu_s) / (st_s["deposits"] / cpu_s),
+            "rel_linf_weight_map_vs_oracle_on_sample": err}
+
+
 def _onchip_ceiling(L, ctx, _lib, value, other, det):
     """The deposit rate the shared-memory accumulation alone allows (3D map:
     one quantity + the weight = 2 channel additions per deposit), from the
@@ -617,7 +677,7 @@ def main():
                     help="time the batched workload alone (for profiler runs)")
     ap.add_argument("--batched-maps", type=int, default=96,
                     help="maps in the batched workload (smaller for profiler captures)")
-    ap.add_argument("--workload", default="clumps_3d", choices=["clumps_3d", "large_hdr"],
+    ap.add_argument("--workload", default="clumps_3d", choices=["clumps_3d", "large_hdr", "healpix"],
                     help="large_hdr: the large-particle projection (2^27 particles, 4096^2), "
                          "FP32C and deterministic against plain FP64 with the error map")
     ap.add_argument("--batched-tuning", default=None,
