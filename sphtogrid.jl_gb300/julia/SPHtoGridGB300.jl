@@ -15,7 +15,7 @@ FP32-compensated deposition.
 """
 module SPHtoGridGB300
 
-using SPHtoGrid: mappingParameters
+using SPHtoGrid: SPHtoGrid, mappingParameters
 using SPHKernels: AbstractSPHKernel, Cubic, Quintic, WendlandC4, WendlandC6, WendlandC8
 using Rotations: RotXYZ  # a dependency of the reference (rotate_particles.jl)
 
@@ -215,6 +215,55 @@ function map_it(pos_in::Array{<:Real}, hsml, mass, rho, bin_q, weights=rho;
                                                  (Ptr{Cvoid},), context())))
     end
     return out
+end
+
+# -------------------------------------------------------------- healpix_map
+
+struct SphgHealpixParams
+    nside::Int64
+    kernel::Int32
+    kernel_dim::Int32
+    calc_mean::Int32
+    dtype::Int32
+end
+
+"""
+    healpix_map(Pos, Hsml, M, Rho, Bin_q, Weights; center=[0.0, 0.0, 0.0],
+                radius_limits=[0.0, Inf], Nside=1024, kernel, calc_mean=true)
+
+The reference's `healpix_map` (healpix_interpolation/main.jl:92-227) with the
+particle loop on the GPU in FP64: `filter_sort_particles` is the reference's
+own (it centres `Pos` in place); the selected particles go to
+`sphg_healpix_map`.  Returns `(allsky_map, weight_map)` as
+`HealpixMap{Float64,RingOrder}`s.
+"""
+function healpix_map(Pos, Hsml, M, Rho, Bin_q, Weights; center::Vector{<:Real}=[0.0, 0.0, 0.0],
+                     radius_limits::Vector{<:Real}=[0.0, Inf], Nside::Integer=1024,
+                     kernel::AbstractSPHKernel, calc_mean::Bool=true, kwargs...)
+    Healpix = Base.require(Base.PkgId(Base.UUID("9f4e344d-96bc-545a-84a3-ae6b9e1b672b"), "Healpix"))
+    CUDA = Base.require(Base.PkgId(Base.UUID("052768ef-5323-5732-b1bb-66c8b64840ba"), "CUDA"))
+    npix = 12 * Nside^2
+    allsky = Healpix.HealpixMap{Float64,Healpix.RingOrder}(Nside)
+    weight = Healpix.HealpixMap{Float64,Healpix.RingOrder}(Nside)
+    (!calc_mean && iszero(sum(Bin_q))) && return allsky, weight
+    pos, hsml, m, rho, q, w = SPHtoGrid.filter_sort_particles(Pos, Hsml, M, Rho, Bin_q, Weights,
+                                                             center, radius_limits, calc_mean)
+    d = map(a -> CUDA.CuArray{Float64}(a), (pos, hsml, m, rho, q, w))
+    da, dw = CUDA.zeros(Float64, npix), CUDA.zeros(Float64, npix)
+    ptr(a) = reinterpret(Ptr{Cvoid}, pointer(a))
+    hp = SphgHealpixParams(Nside, kernel_id(kernel),
+                           hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3),
+                           calc_mean, 1)
+    st = SphgStats()
+    s = ccall((:sphg_healpix_map, libsphgrid), Cint,
+              (Ptr{Cvoid}, Ref{SphgHealpixParams}, Int64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+               Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{SphgStats}),
+              context(), hp, length(hsml), ptr(d[1]), ptr(d[2]), ptr(d[3]), ptr(d[4]), ptr(d[5]),
+              ptr(d[6]), ptr(da), ptr(dw), C_NULL, st)
+    s == 0 || error(unsafe_string(ccall((:sphg_last_error, libsphgrid), Cstring, (Ptr{Cvoid},), context())))
+    allsky.pixels .= Array(da)
+    weight.pixels .= Array(dw)
+    return allsky, weight
 end
 
 # ---------------------------------------------------------------- adjoint
