@@ -710,37 +710,29 @@ __device__ __forceinline__ void prepare_pair(const TiledArgs& A, int r, int ox, 
     for (int k = 0; k < NQ; ++k) H.cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
 }
 
-// The cells of one (record, tile) pair: the intersection's na x nb x nc
-// cells.  Each lane owns a (b, c) column and walks a; with fewer than 32
-// columns, per = 32 / (nb nc) lanes share a column at staggered a.  The index
-// arithmetic per cell is one increment, the column's y and z terms stay in
-// registers, and u and the weight are formed in the same order as in the
-// renormalisation pass.  KERN is a compile-time shape here.
+// The cells of one (record, tile) pair: the intersection's n = na nb nc
+// cells, lane-strided, from the per-axis tables.  KERN is a compile-time
+// shape here.
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
-__device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int na, int nb, int nc, int lbase,
-                                              float hinv, float cw, const float* cq, int nq, int TV, float* hi,
-                                              float* lo, unsigned long long* fx, int lane) {
-  const int nbc = nb * nc;
-  const int per = nbc <= 32 ? 32 / nbc : 1;  // lanes per column
-  const int ncol = nbc <= 32 ? nbc * per : nbc;
-  for (int slot = lane; slot < ncol; slot += 32) {
-    const int col = nbc <= 32 ? slot % nbc : slot;
-    const int a_first = nbc <= 32 ? slot / nbc : 0;
-    const int b = DIMS == 3 ? col / nc : col, c = DIMS == 3 ? col - b * nc : 0;
-    const float2 ey = tab[1][b], ez = tab[2][c];
-    int li = lbase + (a_first * TY + b) * TZ + c;
-    const int dli = per * TY * TZ;
-    for (int a = a_first; a < na; a += per, li += dli) {
-      const float2 ex = tab[0][a];
-      const float u = u_of((ex.x + ey.x) + ez.x, hinv);
-      if (u <= 1.0f) {
-        const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
-        acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+__device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
+                                              float cw, const float* cq, int nq, int TV, float* hi, float* lo,
+                                              unsigned long long* fx, int lane) {
+  const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
+  for (int e = lane; e < n; e += 32) {
+    const int bc = DIMS == 3 ? fdiv(e, inv_nc) : e;  // 2D: nc == 1
+    const int c = DIMS == 3 ? e - bc * nc : 0;
+    const int a = fdiv(bc, inv_nb);
+    const int b = bc - a * nb;
+    const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
+    const float u = u_of((ex.x + ey.x) + ez.x, hinv);
+    if (u <= 1.0f) {
+      const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
+      const int li = lbase + (a * TY + b) * TZ + c;
+      acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
-        for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
-          if (NQ == 0 && k >= nq) break;
-          acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
-        }
+      for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
+        if (NQ == 0 && k >= nq) break;
+        acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
       }
     }
   }
@@ -855,7 +847,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
         // a run-time kernel shape is dispatched once per pair, so the cell
         // loop evaluates a compile-time shape
 #define SPHG_CELLS(K) \
-  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, na, nb, nc, H.lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
+  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, H.lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
         if (KERN >= 0) SPHG_CELLS(KERN >= 0 ? KERN : 0);
         else if (A.kern == 0) SPHG_CELLS(0);
         else if (A.kern == 1) SPHG_CELLS(1);
