@@ -412,8 +412,82 @@ __device__ __forceinline__ TileSpan tile_span(const TiledArgs& A, int4 bx, int4 
   t.nt = (tx1 - t.tx0 + 1) * t.nty * t.ntz;
   return t;
 }
-__device__ __forceinline__ void tile_entry(const TiledArgs& A, const TileSpan& s, int t, int r) {
+
+// Narrows the footprint-local cell ranges [k0[d], k1[d]) of a (record, tile)
+// intersection to the cells whose pixel centres can lie within the kernel
+// support (offset at most h), with margins far above the FP32 rounding of
+// the per-cell test u <= 1, which still decides each cell.  A sphere (disc)
+// fills about a third (three quarters) of its footprint box, and a tile at
+// the box's corner often misses it altogether.  Returns false when no cell
+// of the intersection can be inside.  g = {x, y, z offsets from the
+// footprint start, h}, FP32 record geometry (finite, h > 0).
+template <int DIMS>
+__device__ __forceinline__ void support_min2(const float* f, const int* k0, const int* k1, float* m2) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {  // smallest squared centre offset per axis
+    const float first = f[d] - (float)k0[d] - 0.5f, last = f[d] - (float)(k1[d] - 1) - 0.5f;
+    m2[d] = (d >= DIMS || (last <= 0.0f && first >= 0.0f)) ? 0.0f : fminf(first * first, last * last);
+  }
+}
+
+// Whether any cell of the intersection can be inside the support (the test
+// of support_box without the narrowing: no square root).
+template <int DIMS>
+__device__ __forceinline__ bool support_hits(const float4 g, const int* k0, const int* k1) {
+  const float f[3] = {g.x, g.y, g.z};
+  float m2[3];
+  support_min2<DIMS>(f, k0, k1, m2);
+  return !((m2[0] + m2[1]) + m2[2] > g.w * g.w * (1.0f + 0x1p-10f));
+}
+
+template <int DIMS>
+__device__ __forceinline__ bool support_box(const float4 g, int* k0, int* k1) {
+  const float f[3] = {g.x, g.y, g.z};
+  float m2[3];
+  support_min2<DIMS>(f, k0, k1, m2);
+  const float R2 = g.w * g.w * (1.0f + 0x1p-10f);
+#pragma unroll
+  for (int d = 0; d < DIMS; ++d) {
+    float rem = R2;
+#pragma unroll
+    for (int j = 0; j < DIMS; ++j)
+      if (j != d) rem -= m2[j];
+    if (!(rem >= 0.0f)) return false;
+    const float R = sqrtf(rem) * (1.0f + 0x1p-10f) + 0x1p-10f;
+    const int lo = (int)ceilf(f[d] - 0.5f - R), hi = (int)floorf(f[d] - 0.5f + R);
+    k0[d] = max(k0[d], lo);
+    k1[d] = min(k1[d], hi + 1);
+    if (k1[d] <= k0[d]) return false;
+  }
+  return true;
+}
+
+// Intersection of record box bx (sides dm) with the tile at (ox, oy, oz),
+// footprint-local.
+__device__ __forceinline__ void tile_cut(int4 bx, int4 dm, int ox, int oy, int oz, int tx, int ty, int tz,
+                                         int* k0, int* k1) {
+  k0[0] = max(0, ox - bx.x);
+  k0[1] = max(0, oy - bx.y);
+  k0[2] = max(0, oz - bx.z);
+  k1[0] = min(dm.x, ox + tx - bx.x);
+  k1[1] = min(dm.y, oy + ty - bx.y);
+  k1[2] = min(dm.z, oz + tz - bx.z);
+}
+
+// Appends record r to the list of the t-th tile of its span, unless `tight`
+// (an FP32 record) and no pixel centre of their intersection can lie within
+// the kernel support.  FP64 records may take the fallback weights, which
+// cover every footprint cell, so they keep every tile.
+template <int DIMS>
+__device__ __forceinline__ void tile_entry(const TiledArgs& A, const TileSpan& s, int t, int r, int4 bx, int4 dm,
+                                           bool tight, float4 g) {
   const int ta = t / (s.nty * s.ntz), tb = (t / s.ntz) % s.nty, tc = t % s.ntz;
+  if (tight) {
+    int k0[3], k1[3];
+    tile_cut(bx, dm, (s.tx0 + ta) * A.tdim[0], (s.ty0 + tb) * A.tdim[1], (s.tz0 + tc) * A.tdim[2], A.tdim[0],
+             A.tdim[1], A.tdim[2], k0, k1);
+    if (!support_hits<DIMS>(g, k0, k1)) return;
+  }
   const int64_t tile = ((int64_t)(s.tx0 + ta) * A.ntile[1] + (s.ty0 + tb)) * A.ntile[2] + (s.tz0 + tc);
   const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
   A.pairs[slot] = r;
@@ -427,6 +501,55 @@ __device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int di
     if (dims == 3 && c_gm != 0.0) atomicAdd(&A.st->grid_mass, c_gm);
     for (int c = 0; c < A.pt.nq + 1; ++c)
       if (emax[c] != INT_MIN) atomicMax(&A.exps[c], emax[c]);
+  }
+}
+
+// Tile-list entries of a group of 32 records, lane j holding record r_j
+// (`mine`; `tight`: an FP32 record, whose own lane knows it).  The
+// group's (record, tile) entries are spread over the lanes, so a record
+// with many tiles does not hold up the warp.
+template <int DIMS>
+__device__ __forceinline__ void fill_group(const TiledArgs& A, int64_t r, bool mine, bool tight, int lane) {
+  const unsigned full = 0xffffffffu;
+  int4 bx = make_int4(0, 0, 0, 0), dm = make_int4(0, 0, 0, 0);
+  float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  TileSpan sp = {0, 0, 0, 1, 1, 0};
+  if (mine) {
+    bx = A.box[r];
+    dm = A.dimv[r];
+    g = A.geo[r];
+    sp = tile_span(A, bx, dm);
+  }
+  int incl = sp.nt;  // inclusive scan of the tile counts
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  for (int base = 0; base < total; base += 32) {
+    const int f = base + lane;
+    int j = 0;  // first lane whose inclusive count exceeds f
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int v = __shfl_sync(full, incl, j + step - 1);
+      if (v <= f) j += step;
+    }
+    j = j < 31 ? j : 31;
+    TileSpan s;
+    s.tx0 = __shfl_sync(full, sp.tx0, j);
+    s.ty0 = __shfl_sync(full, sp.ty0, j);
+    s.tz0 = __shfl_sync(full, sp.tz0, j);
+    s.nty = __shfl_sync(full, sp.nty, j);
+    s.ntz = __shfl_sync(full, sp.ntz, j);
+    const int first = __shfl_sync(full, incl - sp.nt, j);
+    const int4 jb = make_int4(__shfl_sync(full, bx.x, j), __shfl_sync(full, bx.y, j), __shfl_sync(full, bx.z, j), 0);
+    const int4 jd = make_int4(__shfl_sync(full, dm.x, j), __shfl_sync(full, dm.y, j), __shfl_sync(full, dm.z, j), 0);
+    const float4 jg = make_float4(__shfl_sync(full, g.x, j), __shfl_sync(full, g.y, j), __shfl_sync(full, g.z, j),
+                                  __shfl_sync(full, g.w, j));
+    const bool jt = __shfl_sync(full, (int)tight, j) != 0;
+    const int64_t jr = __shfl_sync(full, r, j);
+    if (f < total) tile_entry<DIMS>(A, s, f - first, (int)jr, jb, jd, jt, jg);
   }
 }
 
@@ -482,11 +605,7 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
     for (unsigned m = __ballot_sync(0xffffffffu, ill); m; m &= m - 1)
       finish_fp64_warp<DIMS, KERN>(A, g0 + __ffs(m) - 1, lane, c_gm, emax);
     if (mine && !ill) finish_scalar(A, r, my_s, my_c, c_gm, emax);
-    if (mine && !overflow) {
-      const int4 bx = A.box[r];
-      const TileSpan sp = tile_span(A, bx, A.dimv[r]);
-      for (int t = 0; t < sp.nt; ++t) tile_entry(A, sp, t, (int)r);
-    }
+    if (!overflow) fill_group<DIMS>(A, r, mine, !ill, lane);
   }
   flush_stats(A, lane, DIMS, c_gm, emax);
 }
@@ -576,8 +695,11 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
       else if (lane == 0) finish_scalar(A, r, s, comp, c_gm, emax);
       __syncwarp();
       const int4 bx = A.box[r];
-      const TileSpan sp = tile_span(A, bx, A.dimv[r]);
-      for (int t = lane; t < sp.nt; t += 32) tile_entry(A, sp, t, (int)r);
+      const int4 dm = A.dimv[r];
+      const TileSpan sp = tile_span(A, bx, dm);
+      const bool tight = (bx.w & kRecFP64) == 0;
+      const float4 g = A.geo[r];
+      for (int t = lane; t < sp.nt; t += 32) tile_entry<DIMS>(A, sp, t, (int)r, bx, dm, tight, g);
     }
   }
   flush_stats(A, lane, DIMS, c_gm, emax);
@@ -686,18 +808,24 @@ __device__ __forceinline__ void prepare_pair(const TiledArgs& A, int r, int ox, 
                                              const int* s_shift, PairHdr& H) {
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
-  const int a0 = max(0, ox - bx.x), a1 = min(dm.x, ox + TX - bx.x);
-  const int b0 = max(0, oy - bx.y), b1 = min(dm.y, oy + TY - bx.y);
-  const int c0 = DIMS == 3 ? max(0, oz - bx.z) : 0, c1 = DIMS == 3 ? min(dm.z, oz + TZ - bx.z) : 1;
+  int k0[3], k1[3];
+  tile_cut(bx, dm, ox, oy, oz, TX, TY, TZ, k0, k1);
+  const bool fp64 = (bx.w & kRecFP64) != 0;
+  float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (!fp64) {
+    // FP32 record: only the cells that can be inside the kernel support
+    g = A.geo[r];
+    if (!support_box<DIMS>(g, k0, k1)) k1[0] = k0[0];  // none: an empty pair
+  }
+  const int a0 = k0[0], b0 = k0[1], c0 = k0[2];
   const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
   H.a0 = a0;
   H.b0 = b0;
   H.c0 = c0;
-  H.dims = (a1 - a0) | ((b1 - b0) << 8) | ((c1 - c0) << 16) | ((bx.w & kRecFP64) ? (1 << 24) : 0);
+  H.dims = (k1[0] - a0) | ((k1[1] - b0) << 8) | ((k1[2] - c0) << 16) | (fp64 ? (1 << 24) : 0);
   H.lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
   H.r = r;
-  if (bx.w & kRecFP64) return;
-  const float4 g = A.geo[r];
+  if (fp64) return;
   H.fx = g.x;
   H.fy = g.y;
   H.fz = g.z;
@@ -755,7 +883,9 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // after an overflow of the pair list the lists are incomplete: deposit
   // nothing (the host grows the list and maps again)
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
-  const long long p0 = A.tile_start[t], p1 = overflow ? p0 : A.tile_start[t + 1];
+  // the list holds the pairs the renormalisation pass kept (tile_fill of
+  // the tile_count slots counted for the whole footprint boxes)
+  const long long p0 = A.tile_start[t], p1 = overflow ? p0 : p0 + A.tile_fill[t];
   // channel scales (powers of two): 2^s_shift as double for the flush
   double* s_scale = sh.scale;
   double* s_unscale = sh.unscale;
@@ -818,6 +948,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       const int na = dims & 0xff, nb = (dims >> 8) & 0xff, nc = (dims >> 16) & 0xff;
       const int n = na * nb * nc;
       const int a0 = H.a0, b0 = H.b0, c0 = H.c0;
+      if (n == 0) continue;  // no cell within the kernel support (uniform: H is shared)
       if (dims & (1 << 24)) {
         const int r = H.r;
         const int4 bx = A.box[r];
