@@ -71,10 +71,11 @@ __global__ void __launch_bounds__(1024) kb_scan(BatchDev B) {
 __global__ void __launch_bounds__(256, 4) kb_norm(BatchDev B) {
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  __shared__ NormShared sh;
   for (int m = 0; m < B.n_maps; ++m) {
     const TiledArgs& A = B.maps[m];
-    if (A.mp.dims == 2) norm_records<2, -1>(A, wid, nw, threadIdx.x & 31);
-    else norm_records<3, -1>(A, wid, nw, threadIdx.x & 31);
+    if (A.mp.dims == 2) norm_records<2, -1>(A, wid, nw, threadIdx.x & 31, sh);
+    else norm_records<3, -1>(A, wid, nw, threadIdx.x & 31, sh);
   }
 }
 

@@ -216,6 +216,13 @@ __device__ __forceinline__ void cell_term_plane(int kern, float2 pxy, float2 ez,
   }
 }
 
+// Per-warp scratch of the renormalisation pass (one instance per kernel,
+// shared by every specialisation it inlines).
+struct NormShared {
+  float2 tabs[8][3][kNormTab];
+  float2 plane[8][kNormPlane];
+};
+
 // The whole footprint of one record from per-axis tables filled by the warp
 // (3D footprints with few columns: from a plane table too, one index
 // division per cell instead of two).
@@ -231,15 +238,30 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
   }
   __syncwarp();
   if (DIMS == 3 && dm.x * dm.y <= kNormPlane) {
+    // Only the columns whose (x, y) offset can be within h: a column with
+    // sx + sy above h^2 (with a margin far above the FP32 rounding of the
+    // per-cell test u <= 1) has no cell inside the support.  A sphere's
+    // columns fill about three quarters of its footprint's.
     const int nab = dm.x * dm.y;
     const float inv_ny = inv_small(dm.y);
-    for (int i = lane; i < nab; i += 32) {
-      const int a = fdiv(i, inv_ny), b = i - a * dm.y;
-      const float2 ex = tab[0][a], ey = tab[1][b];
-      plane[i] = make_float2(ex.x + ey.x, ex.y * ey.y);
+    const float R2 = h * h * (1.0f + 0x1p-10f);
+    int ncol = 0;
+    for (int i0 = 0; i0 < nab; i0 += 32) {
+      const int i = i0 + lane;
+      float2 pxy = make_float2(0.0f, 0.0f);
+      bool keep = false;
+      if (i < nab) {
+        const int a = fdiv(i, inv_ny), b = i - a * dm.y;
+        const float2 ex = tab[0][a], ey = tab[1][b];
+        pxy = make_float2(ex.x + ey.x, ex.y * ey.y);
+        keep = !(pxy.x > R2);
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (keep) plane[ncol + __popc(bal & lanemask_lt())] = pxy;
+      ncol += __popc(bal);
     }
     __syncwarp();
-    const int F = nab * dm.z;
+    const int F = ncol * dm.z;
     const float inv_nz = inv_small(dm.z);
     for (int f = lane; f < F; f += 32) {
       const int ab = fdiv(f, inv_nz), c = f - ab * dm.z;
@@ -560,16 +582,14 @@ __device__ __forceinline__ void fill_group(const TiledArgs& A, int64_t r, bool m
 // fraction of FP32 throughput on GB300) costs one warp instruction sequence
 // per 32 records.  Each lane also writes its record's tile-list entries.
 template <int DIMS, int KERN>
-__device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int lane) {
+__device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int lane, NormShared& sh) {
   const int nrec = *A.n_rec;
   const bool overflow = (A.st->flags & kFlagOverflow) != 0;
   double c_gm = 0.0;
   int emax[kMaxQ + 1];
   for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
-  __shared__ float2 tabs[8][3][kNormTab];  // one set per warp of a 256-thread CTA
-  __shared__ float2 planes[8][DIMS == 3 ? kNormPlane : 1];
-  float2(*tab)[kNormTab] = tabs[(threadIdx.x >> 5) & 7];
-  float2* plane = planes[(threadIdx.x >> 5) & 7];
+  float2(*tab)[kNormTab] = sh.tabs[(threadIdx.x >> 5) & 7];  // one set per warp of a 256-thread CTA
+  float2* plane = sh.plane[(threadIdx.x >> 5) & 7];
   for (int64_t g0 = wid * 32; g0 < nrec; g0 += nw * 32) {
     const int cnt = nrec - g0 < 32 ? (int)(nrec - g0) : 32;
     float my_s = 0.0f, my_c = 0.0f, my_u = 0.0f;
@@ -613,8 +633,9 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
 // K3: one warp per group of 32 small records.
 template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256, 4) k_norm_fill(TiledArgs A) {
+  __shared__ NormShared sh;
   norm_records<DIMS, KERN>(A, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
-                           ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
+                           ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31, sh);
 }
 
 // K3L phase 1: every CTA takes chunks of kChunkCells cells of the large
