@@ -1054,10 +1054,10 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-// Launch bounds by measurement: the deposit is latency-bound, so resident
-// warps matter more than the registers given up (3D: eight CTAs per SM;
-// 2D carries up to four channels per cell and keeps six).
-__global__ void __launch_bounds__(256, DIMS == 3 ? 8 : 6) k_deposit(TiledArgs A) {
+// Launch bounds by measurement: six CTAs per SM (40 registers).  Eight (32
+// registers) spill the per-pair support narrowing and cell loop to local
+// memory; five leave too few warps to hide the shared-memory latency.
+__global__ void __launch_bounds__(256, 6) k_deposit(TiledArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DepositShared sh;
   deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw, sh);
