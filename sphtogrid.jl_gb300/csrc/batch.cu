@@ -68,33 +68,55 @@ __global__ void __launch_bounds__(1024) kb_scan(BatchDev B) {
   scan_tiles(B.maps[blockIdx.x], part);
 }
 
+// The renormalisation phase runs once per (dimensions, kernel shape) that
+// the batch holds, over that shape's maps: each launch evaluates one
+// compile-time shape, so its code stays small (one launch over every shape
+// inlined all of them and stalled on instruction fetch).
+template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256, 4) kb_norm(BatchDev B) {
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   __shared__ NormShared sh;
   for (int m = 0; m < B.n_maps; ++m) {
     const TiledArgs& A = B.maps[m];
-    if (A.mp.dims == 2) norm_records<2, -1>(A, wid, nw, threadIdx.x & 31, sh);
-    else norm_records<3, -1>(A, wid, nw, threadIdx.x & 31, sh);
+    if (A.mp.dims == DIMS && A.kern == KERN) norm_records<DIMS, KERN>(A, wid, nw, threadIdx.x & 31, sh);
   }
 }
 
+template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256) kb_large_partials(BatchDev B) {
   __shared__ float red[3][8];
   for (int m = 0; m < B.n_maps; ++m) {
     const TiledArgs& A = B.maps[m];
-    if (A.mp.dims == 2) large_partials<2, -1>(A, blockIdx.x, gridDim.x, red);
-    else large_partials<3, -1>(A, blockIdx.x, gridDim.x, red);
+    if (A.mp.dims == DIMS && A.kern == KERN) large_partials<DIMS, KERN>(A, blockIdx.x, gridDim.x, red);
   }
 }
 
+template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256) kb_large_finish(BatchDev B) {
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int m = 0; m < B.n_maps; ++m) {
     const TiledArgs& A = B.maps[m];
-    if (A.mp.dims == 2) large_finish<2, -1>(A, wid, nw, threadIdx.x & 31);
-    else large_finish<3, -1>(A, wid, nw, threadIdx.x & 31);
+    if (A.mp.dims == DIMS && A.kern == KERN) large_finish<DIMS, KERN>(A, wid, nw, threadIdx.x & 31);
+  }
+}
+
+template <int DIMS, int KERN>
+void launch_norm_shape(const BatchDev& d, int num_sms, cudaStream_t s) {
+  kb_norm<DIMS, KERN><<<num_sms * 16, 256, 0, s>>>(d);
+  kb_large_partials<DIMS, KERN><<<num_sms * 4, 256, 0, s>>>(d);
+  kb_large_finish<DIMS, KERN><<<num_sms * 4, 256, 0, s>>>(d);
+}
+
+template <int DIMS>
+void launch_norm_dims(int kern, const BatchDev& d, int num_sms, cudaStream_t s) {
+  switch (kern) {
+    case 0: launch_norm_shape<DIMS, 0>(d, num_sms, s); break;
+    case 1: launch_norm_shape<DIMS, 1>(d, num_sms, s); break;
+    case 2: launch_norm_shape<DIMS, 2>(d, num_sms, s); break;
+    case 3: launch_norm_shape<DIMS, 3>(d, num_sms, s); break;
+    default: launch_norm_shape<DIMS, 4>(d, num_sms, s); break;
   }
 }
 
@@ -191,6 +213,7 @@ struct BatchPlan {
   size_t smem = 0;
   bool det = false;
   int k1_grid = 0;
+  std::vector<int> shapes;  // (dimensions, kernel shape) pairs present: dims * 8 + shape
 };
 
 }  // namespace sphg
@@ -315,6 +338,10 @@ int build_plan(sphg_batch* b) {
   }
   for (int i = 0; i < nm; ++i) p.tile_base[i + 1] = p.tile_base[i] + b->maps[p.order[i]].n_tiles;
   p.k1_grid = p.blk_base[nm];
+  p.shapes.clear();  // kernel ids are validated (0-4) when the maps are added
+  for (int m = 0; m < nm; ++m) p.shapes.push_back(b->maps[m].desc.opt.dimensions * 8 + b->maps[m].desc.opt.kernel);
+  std::sort(p.shapes.begin(), p.shapes.end());
+  p.shapes.erase(std::unique(p.shapes.begin(), p.shapes.end()), p.shapes.end());
   for (int m = 0; m < nm; ++m) {
     const BatchMapHost& M = b->maps[m];
     const sphg_map_desc& D = M.desc;
@@ -427,9 +454,10 @@ int enqueue(sphg_batch* b, cudaStream_t s) {
   BCK(cudaMemsetAsync(p.d_status, 0, (size_t)nm * sizeof(DevStatus) + sizeof(unsigned long long), s));
   kb_prep<<<p.k1_grid, 256, 0, s>>>(p.dev);
   kb_scan<<<nm, 1024, 0, s>>>(p.dev);
-  kb_norm<<<b->num_sms * 16, 256, 0, s>>>(p.dev);
-  kb_large_partials<<<b->num_sms * 4, 256, 0, s>>>(p.dev);
-  kb_large_finish<<<b->num_sms * 4, 256, 0, s>>>(p.dev);
+  for (const int shape : p.shapes) {  // dims * 8 + kernel shape
+    if (shape >> 3 == 2) launch_norm_dims<2>(shape & 7, p.dev, b->num_sms, s);
+    else launch_norm_dims<3>(shape & 7, p.dev, b->num_sms, s);
+  }
   if (!launch_kb_deposit(p.tile_x, p.tile_y, p.dev, p.det, b->num_sms * p.ctas_per_sm, p.smem, s))
     return bfail(b, SPHG_ERR_ARG, "tile shape must be 16x16, 32x16 or 32x32");
   BCK(cudaGetLastError());
