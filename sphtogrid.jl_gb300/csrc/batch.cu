@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -124,9 +125,9 @@ void launch_norm_dims(int kern, const BatchDev& d, int num_sms, cudaStream_t s) 
 // persistent kernel dispatches among several specialisations, and a call per
 // tile keeps each one's register use inside its own cell loop.
 template <int DIMS, int NQ, int TX, int TY, int TZ, bool DET>
-__device__ __noinline__ void tile_call(const TiledArgs& A, long long t, unsigned char* smem_raw,
+__device__ __noinline__ void tile_call(const TiledArgs& A, long long t, int chunk, unsigned char* smem_raw,
                                        DepositShared& sh) {
-  deposit_tile<DIMS, -1, NQ, TX, TY, TZ, DET>(A, t, smem_raw, sh);
+  deposit_tile<DIMS, -1, NQ, TX, TY, TZ, DET>(A, t, smem_raw, sh, chunk);
 }
 
 // The persistent deposit: every CTA takes the next tile from the queue until
@@ -144,18 +145,22 @@ __global__ void __launch_bounds__(256, 6) kb_deposit(BatchDev B) {
     if (t >= B.total_tiles) break;
     const int pos = find_seg_ll(B.tile_base, B.n_maps, t);
     const TiledArgs& A = B.maps[B.order[pos]];
-    const long long local = t - B.tile_base[pos];
+    // a split map's queue slots are (chunk, tile), chunk-major, so the
+    // chunks of one tile run apart in time
+    const long long slot = t - B.tile_base[pos];
+    const long long local = A.split > 1 ? slot % A.n_tiles : slot;
+    const int chunk = A.split > 1 ? (int)(slot / A.n_tiles) : 0;
     // the map's channel count as a compile-time constant keeps the per-pair
     // factors in registers (3D maps carry one quantity)
     if (A.mp.dims == 3) {
-      tile_call<3, 1, kTile3X, kTile3Y, kTile3Z, DET>(A, local, smem_raw, sh);
+      tile_call<3, 1, kTile3X, kTile3Y, kTile3Z, DET>(A, local, chunk, smem_raw, sh);
     } else {
       switch (A.pt.nq) {
-        case 1: tile_call<2, 1, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
-        case 2: tile_call<2, 2, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
-        case 3: tile_call<2, 3, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
-        case 4: tile_call<2, 4, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
-        default: tile_call<2, 0, TX, TY, 1, DET>(A, local, smem_raw, sh); break;
+        case 1: tile_call<2, 1, TX, TY, 1, DET>(A, local, chunk, smem_raw, sh); break;
+        case 2: tile_call<2, 2, TX, TY, 1, DET>(A, local, chunk, smem_raw, sh); break;
+        case 3: tile_call<2, 3, TX, TY, 1, DET>(A, local, chunk, smem_raw, sh); break;
+        case 4: tile_call<2, 4, TX, TY, 1, DET>(A, local, chunk, smem_raw, sh); break;
+        default: tile_call<2, 0, TX, TY, 1, DET>(A, local, chunk, smem_raw, sh); break;
       }
     }
   }
@@ -185,6 +190,13 @@ bool launch_kb_deposit(int tx, int ty, const BatchDev& B, bool det, int grid, si
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// Pairs per (chunk of a) tile above which a map's tiles are split over
+// several CTAs, and the most chunks per tile.  A map of many particles on
+// few pixels has few, heavy tiles; one CTA each would leave the rest of
+// the GPU idle while they finish.
+constexpr double kSplitPairs = 4096.0;
+constexpr int kMaxSplit = 64;
+
 }  // namespace
 
 // ------------------------------------------------------------------ host
@@ -194,7 +206,17 @@ struct BatchMapHost {
   sphg_params cpar;
   int64_t n_tiles = 0;
   long long pair_cap = 0, chunk_cap = 0;
+  int split = 1;  // chunks per tile (CTAs sharing each tile's pairs)
 };
+
+// Chunks per tile of a map from its expected pairs per tile (about 1.5
+// tiles per particle in 2D, 3 in 3D, for footprints small next to a tile).
+inline int split_of(const BatchMapHost& M) {
+  if (M.n_tiles <= 0) return 1;
+  const double per_tile = (double)M.desc.parts.n * (M.desc.opt.dimensions == 2 ? 1.5 : 3.0) / (double)M.n_tiles;
+  const double k = std::ceil(per_tile / kSplitPairs);
+  return k < 1.0 ? 1 : (k > kMaxSplit ? kMaxSplit : (int)k);
+}
 
 struct BatchPlan {
   int tile_x = 16, tile_y = 16, ctas_per_sm = 4, large_cells = (int)kLargeCells;
@@ -214,6 +236,7 @@ struct BatchPlan {
   bool det = false;
   int k1_grid = 0;
   std::vector<int> shapes;  // (dimensions, kernel shape) pairs present: dims * 8 + shape
+  std::vector<std::pair<char*, size_t>> zero;  // split maps' partial sums, zeroed per run
 };
 
 }  // namespace sphg
@@ -263,6 +286,8 @@ int build_plan(sphg_batch* b) {
   const int nm = (int)b->maps.size();
   free_plan(p);
   p.args.assign(nm, TiledArgs());
+  p.zero.clear();
+  for (BatchMapHost& M : b->maps) M.split = split_of(M);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     size_t o = off;
@@ -270,7 +295,7 @@ int build_plan(sphg_batch* b) {
     return o;
   };
   struct Off {
-    size_t box, dim, geo, cp, cpm, cpe, aux, qv, start, pairs, large, lstart, part;
+    size_t box, dim, geo, cp, cpm, cpe, aux, qv, start, pairs, large, lstart, part, acc;
   };
   std::vector<Off> offs(nm);
   // shared regions first: counters, exponents, bounds, statuses + queue
@@ -305,6 +330,10 @@ int build_plan(sphg_batch* b) {
     o.large = take(cap * sizeof(int));
     o.lstart = take((cap + 1) * sizeof(long long));
     o.part = take(M.chunk_cap * sizeof(float4));
+    // tiles split over several CTAs: the raw partial sums and chunk counters
+    const int64_t P = M.desc.par.Npixels[0];
+    const int64_t PD = M.desc.opt.dimensions == 2 ? P * P : P * P * P;
+    o.acc = M.split > 1 ? take((size_t)PD * (nq + 1) * sizeof(double) + M.n_tiles * sizeof(int)) : 0;
     const size_t tv = M.desc.opt.dimensions == 2 ? (size_t)p.tile_x * p.tile_y
                                                  : (size_t)kTile3X * kTile3Y * kTile3Z;
     smem = std::max(smem, 2 * (size_t)(nq + 1) * tv * sizeof(float));
@@ -336,7 +365,10 @@ int build_plan(sphg_batch* b) {
     const int64_t n = M.desc.parts.n;
     p.blk_base[m + 1] = p.blk_base[m] + (int)std::max<int64_t>(1, (n + 255) / 256);
   }
-  for (int i = 0; i < nm; ++i) p.tile_base[i + 1] = p.tile_base[i] + b->maps[p.order[i]].n_tiles;
+  for (int i = 0; i < nm; ++i) {
+    const BatchMapHost& M = b->maps[p.order[i]];
+    p.tile_base[i + 1] = p.tile_base[i] + M.n_tiles * M.split;
+  }
   p.k1_grid = p.blk_base[nm];
   p.shapes.clear();  // kernel ids are validated (0-4) when the maps are added
   for (int m = 0; m < nm; ++m) p.shapes.push_back(b->maps[m].desc.opt.dimensions * 8 + b->maps[m].desc.opt.kernel);
@@ -418,6 +450,14 @@ int build_plan(sphg_batch* b) {
     A.det = p.det ? 1 : 0;
     A.st = p.d_status + m;
     A.out = D.out;
+    A.split = M.split;
+    if (M.split > 1) {
+      const int64_t PD = dims == 2 ? P * P : P * P * P;
+      const size_t acc_bytes = (size_t)PD * (D.parts.n_q + 1) * sizeof(double);
+      A.acc = (double*)(base + o.acc);
+      A.done = (int*)(base + o.acc + acc_bytes);
+      p.zero.push_back({base + o.acc, acc_bytes + M.n_tiles * sizeof(int)});
+    }
     const bool raw = D.opt.raw_accumulator || (dims == 2 && D.opt.return_both_maps);
     A.mode = raw ? 1 : (dims == 3 ? 2 : 0);
     A.reduce = D.opt.reduce_image;
@@ -452,6 +492,7 @@ int enqueue(sphg_batch* b, cudaStream_t s) {
   BCK(cudaMemsetAsync(p.counters, 0, p.counters_bytes, s));
   BCK(cudaMemsetAsync(p.exps, 0x80, (size_t)nm * (kMaxQ + 1) * sizeof(int), s));
   BCK(cudaMemsetAsync(p.d_status, 0, (size_t)nm * sizeof(DevStatus) + sizeof(unsigned long long), s));
+  for (const auto& z : p.zero) BCK(cudaMemsetAsync(z.first, 0, z.second, s));
   kb_prep<<<p.k1_grid, 256, 0, s>>>(p.dev);
   kb_scan<<<nm, 1024, 0, s>>>(p.dev);
   for (const int shape : p.shapes) {  // dims * 8 + kernel shape

@@ -85,6 +85,13 @@ struct TiledArgs {
   int mode;         // 0: 2D reduced, 1: raw (P^D, nq+1) accumulator, 2: 3D reduced
   int reduce;       // 2D reduce_image
   int w_is_one;     // 3D !reduce_image
+  // tiles split over several CTAs (split > 1): chunk c of a tile deposits
+  // pairs [c n / split, (c + 1) n / split) of its n and adds its partial
+  // sums to `acc`; the tile's last chunk writes the output from there
+  int split;
+  double* acc;      // raw (P^D, nq+1) partial sums: FP64, or the int64 fixed-point
+                    // bits in the deterministic mode (one scale per tile)
+  int* done;        // chunks finished per tile
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -810,7 +810,49 @@ struct DepositShared {
   double bnd[kMaxQ + 1][8];  // deterministic mode: per-warp tile bounds
   float2 tabs[8][3][32];     // per-warp axis tables of the current pair
   PairHdr hdr[8][kPairBatch];  // per-warp batch of prepared pairs
+  int last;                  // split tile: this CTA finished it
 };
+
+// Writes one output pixel (i, j, k) from its W and channel values q(c) in
+// the output's layout (raw accumulator, 3D reduced or 2D reduced).
+template <int DIMS, class QFn>
+__device__ __forceinline__ void store_cell(const TiledArgs& A, int64_t P, int64_t PD, int i, int j, int k, int nq,
+                                           double W, QFn q) {
+  if (A.mode == 1) {  // raw (P^D, nq+1) accumulator
+    const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
+    A.out[row + (int64_t)nq * PD] = W;
+    for (int c = 0; c < nq; ++c) A.out[row + c * PD] = q(c);
+  } else if (DIMS == 3) {
+    double Q = q(0);
+    if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
+    A.out[((int64_t)i * P + j) * P + k] = Q;
+  } else {
+    for (int c = 0; c < nq; ++c) {
+      double Q = q(c);
+      if (A.reduce && W > 0.0) Q /= W;
+      A.out[(int64_t)i + P * j + PD * c] = Q;
+    }
+  }
+}
+
+// Tile cell v of the flush walk: its tile-local index li and pixel (i, j, k).
+// The reduced 2D output is x-fastest, so that walk is x-fastest.
+template <int DIMS, int TX, int TY, int TZ>
+__device__ __forceinline__ void flush_cell(const TiledArgs& A, int v, int ox, int oy, int oz, bool xfast, int& li,
+                                           int& i, int& j, int& k) {
+  if (DIMS == 2 && xfast) {
+    const int ix = v % TX, iy = v / TX;
+    li = ix * TY + iy;
+    i = ox + ix;
+    j = oy + iy;
+    k = 0;
+  } else {
+    li = v;
+    i = ox + v / (TY * TZ);
+    j = oy + (v / TZ) % TY;
+    k = oz + v % TZ;
+  }
+}
 
 // FP32 factor of channel k of record r: cpm * q * 2^(cpe + shift), with q
 // split into mantissa and exponent so no intermediate leaves the FP32 range
@@ -872,7 +914,9 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
     const int c = DIMS == 3 ? e - bc * nc : 0;
     const int a = fdiv(bc, inv_nb);
     const int b = bc - a * nb;
-    const float2 ex = tab[0][a], ey = tab[1][b], ez = tab[2][c];
+    // 2D: the z term is the constant {0, 1} (the same u and weight as the
+    // renormalisation pass forms)
+    const float2 ex = tab[0][a], ey = tab[1][b], ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
     const float u = u_of((ex.x + ey.x) + ez.x, hinv);
     if (u <= 1.0f) {
       const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
@@ -888,7 +932,8 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-__device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh) {
+__device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh,
+                             int chunk = 0) {
   constexpr int TV = TX * TY * TZ;
   const int nq = NQ > 0 ? NQ : A.pt.nq;
   const int nch = nq + 1;
@@ -907,6 +952,10 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // the list holds the pairs the renormalisation pass kept (tile_fill of
   // the tile_count slots counted for the whole footprint boxes)
   const long long p0 = A.tile_start[t], p1 = overflow ? p0 : p0 + A.tile_fill[t];
+  const bool split = A.split > 1;
+  // this CTA's pairs: all of the tile's, or its chunk of them
+  const long long c0 = split ? p0 + (p1 - p0) * chunk / A.split : p0;
+  const long long c1 = split ? p0 + (p1 - p0) * (chunk + 1) / A.split : p1;
   // channel scales (powers of two): 2^s_shift as double for the flush
   double* s_scale = sh.scale;
   double* s_unscale = sh.unscale;
@@ -956,12 +1005,12 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // lanes prepares one pair of the next batch (their record loads are in
   // flight together, and the per-pair arithmetic runs once per batch);
   // phase B: the warp deposits the batch pair by pair from the headers.
-  for (long long sb = p0 + warp; sb < p1; sb += (long long)nwarp * kPairBatch) {
+  for (long long sb = c0 + warp; sb < c1; sb += (long long)nwarp * kPairBatch) {
     const long long sj = sb + (long long)lane * nwarp;
-    if (lane < kPairBatch && sj < p1)
+    if (lane < kPairBatch && sj < c1)
       prepare_pair<DIMS, NQ, TX, TY, TZ>(A, A.pairs[sj], ox, oy, oz, nq, s_shift, hdr[lane]);
     __syncwarp();
-    const long long left = (p1 - sb + nwarp - 1) / nwarp;
+    const long long left = (c1 - sb + nwarp - 1) / nwarp;
     const int cnt = left < kPairBatch ? (int)left : kPairBatch;
     for (int j = 0; j < cnt; ++j) {
       const PairHdr& H = hdr[j];
@@ -1013,42 +1062,56 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     __syncwarp();  // the headers are refilled for the next batch
   }
   __syncthreads();
-  // flush: FP64 values straight into the output layout
   const int64_t P = A.mp.P;
   const int64_t PD = DIMS == 2 ? P * P : P * P * P;
   const double inv_w = s_unscale[nq];
-  for (int v = threadIdx.x; v < TV; v += blockDim.x) {
-    int li, i, j, k;
-    if (DIMS == 2 && A.mode == 0) {
-      // reduced 2D output is x-fastest: walk the tile x-fastest
-      const int ix = v % TX, iy = v / TX;
-      li = ix * TY + iy;
-      i = ox + ix;
-      j = oy + iy;
-      k = 0;
-    } else {
-      li = v;
-      i = ox + v / (TY * TZ);
-      j = oy + (v / TZ) % TY;
-      k = oz + v % TZ;
-    }
-    if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
-    const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
-    if (A.mode == 1) {  // raw (P^D, nq+1) accumulator
+  if (split) {
+    // add this chunk's sums to the tile's raw partial sums (exact int64 in
+    // the deterministic mode: every chunk of the tile has the same scale)
+    for (int v = threadIdx.x; v < TV; v += blockDim.x) {
+      int li, i, j, k;
+      flush_cell<DIMS, TX, TY, TZ>(A, v, ox, oy, oz, false, li, i, j, k);
+      if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
       const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
-      A.out[row + (int64_t)nq * PD] = W;
-      for (int c = 0; c < nq; ++c) A.out[row + c * PD] = cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c];
-    } else if (DIMS == 3) {
-      double Q = cell_value<DET>(hi, lo, fx, li) * s_unscale[0];
-      if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
-      A.out[((int64_t)i * P + j) * P + k] = Q;
-    } else {
-      for (int c = 0; c < nq; ++c) {
-        double Q = cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c];
-        if (A.reduce && W > 0.0) Q /= W;
-        A.out[(int64_t)i + P * j + PD * c] = Q;
+      for (int c = 0; c <= nq; ++c) {
+        if (DET) {
+          const unsigned long long x = fx[c * TV + li];
+          if (x) atomicAdd((unsigned long long*)A.acc + row + c * PD, x);
+        } else {
+          const double x = cell_value<DET>(hi, lo, fx, c * TV + li);
+          if (x != 0.0) atomicAdd(A.acc + row + c * PD, x * s_unscale[c]);
+        }
       }
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) sh.last = atomicAdd(A.done + t, 1) == A.split - 1;
+    __syncthreads();
+    if (sh.last) {  // every chunk of the tile has added its sums: write the output
+      __threadfence();
+      for (int v = threadIdx.x; v < TV; v += blockDim.x) {
+        int li, i, j, k;
+        flush_cell<DIMS, TX, TY, TZ>(A, v, ox, oy, oz, DIMS == 2 && A.mode == 0, li, i, j, k);
+        if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
+        const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
+        auto sum = [&](int c) {
+          if (DET) return (double)(long long)__ldcg((const unsigned long long*)A.acc + row + c * PD) * s_unscale[c];
+          return __ldcg(A.acc + row + c * PD);
+        };
+        store_cell<DIMS>(A, P, PD, i, j, k, nq, sum(nq), sum);
+      }
+    }
+    __syncthreads();  // the shared accumulators are reused by the next tile
+    return;
+  }
+  // flush: FP64 values straight into the output layout
+  for (int v = threadIdx.x; v < TV; v += blockDim.x) {
+    int li, i, j, k;
+    flush_cell<DIMS, TX, TY, TZ>(A, v, ox, oy, oz, DIMS == 2 && A.mode == 0, li, i, j, k);
+    if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
+    const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
+    store_cell<DIMS>(A, P, PD, i, j, k, nq, W,
+                     [&](int c) { return cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c]; });
   }
   __syncthreads();  // the shared accumulators are reused by the next tile
 }
