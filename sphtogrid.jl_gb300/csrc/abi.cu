@@ -26,6 +26,8 @@ struct sphg_context {
   size_t pair_cap = 0;                  // FP32C tile-pair list capacity (grow-only)
   size_t chunk_cap = 0;                 // FP32C large-record chunk capacity (grow-only)
   cudaEvent_t ev[5] = {};               // phase timing events
+  double* hp_centres = nullptr;         // HEALPix pixel-centre table of hp_nside
+  int64_t hp_nside = 0;
 };
 
 namespace {
@@ -185,6 +187,7 @@ int sphg_context_destroy(sphg_context* ctx) {
     std::lock_guard<std::mutex> lk(ctx->mu);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->ws) cudaFree(ctx->ws);
+    if (ctx->hp_centres) cudaFree(ctx->hp_centres);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     for (int k = 0; k < 5; ++k)
@@ -636,9 +639,29 @@ int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n
   DeviceGuard g(ctx->device);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
+  // the pixel-centre table (3 FP64 per pixel, kept for the next call of the
+  // same Nside) up to Nside 4096 (4.8 GB); above that, or when it cannot be
+  // allocated, the centres are computed per use
+  bool fill = false;
+  if (n > 0 && ns <= 4096 && ctx->hp_nside != ns) {
+    if (ctx->hp_centres) {
+      CK(cudaStreamSynchronize(s));
+      CK(cudaFree(ctx->hp_centres));
+      ctx->hp_centres = nullptr;
+      ctx->hp_nside = 0;
+    }
+    if (cudaMalloc(&ctx->hp_centres, (size_t)12 * ns * ns * 3 * sizeof(double)) == cudaSuccess) {
+      ctx->hp_nside = ns;
+      fill = true;
+    } else {
+      cudaGetLastError();
+      ctx->hp_centres = nullptr;
+    }
+  }
+  double* centres = ctx->hp_nside == ns ? ctx->hp_centres : nullptr;
   if (n > 0)
     sphg::launch_healpix(ns, hp->kernel, hp->kernel_dim, hp->calc_mean, hp->dtype, n, pos, hsml, mass, rho, bin_q,
-                         weights, allsky, weight, ctx->d_status, ctx->num_sms, s);
+                         weights, allsky, weight, centres, fill, ctx->d_status, ctx->num_sms, s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

@@ -170,7 +170,7 @@ __device__ __forceinline__ void hp_ring_range(const HpDisc& D, const HpRing& R, 
 }
 
 struct HpParticle {
-  double p[3], dx, proj, hinv, area_norm, q, scale;  // scale: (ang_pix dx)^-2
+  double p[3], dx, dxinv, proj, hinv, area_norm, q, scale;  // scale: (ang_pix dx)^-2
   int fallback;
 };
 
@@ -179,7 +179,9 @@ __device__ __forceinline__ void hp_terms(int KERN_RT, int kdim, const HpParticle
                                          double ang_pix, double* wk, double* a, bool* inside) {
   double d = 0.0;
   for (int c = 0; c < 3; ++c) d += P.p[c] * pc[c];
-  const double ddx = acos(fmin(d / P.dx, 1.0));
+  // d / |p| as a product with the reciprocal (within an ulp of the
+  // quotient: where acos amplifies that, u is near 0 and the kernel flat)
+  const double ddx = acos(fmin(d * P.dxinv, 1.0));
   const double u = ddx * P.hinv;
   *a = fmax(0.0, fmin(ang_pix, fabs(P.proj - (ddx - 0.5 * ang_pix)))) / ang_pix * P.scale;
   *inside = u <= 1.0;
@@ -205,8 +207,36 @@ struct HpArgs {
   int kernel, kdim, calc_mean, dtype;
   const void *pos, *hsml, *m, *rho, *q, *w;  // pos: 3 per particle
   double *allsky, *weight;
+  const double* centres;  // pixel-centre unit vectors (3 per pixel), or NULL
   DevStatus* st;
 };
+
+// Centre of in-ring pixel kk of ring R: from the precomputed table (the same
+// arithmetic, once per pixel instead of twice per particle and pixel).
+__device__ __forceinline__ void pixel_centre(const HpArgs& H, const HpRing& R, int64_t kk, double pc[3]) {
+  if (H.centres) {
+    const double* c = H.centres + 3 * (R.first + kk);
+    pc[0] = c[0];
+    pc[1] = c[1];
+    pc[2] = c[2];
+  } else {
+    hp_centre(R, kk, pc);
+  }
+}
+
+// The table of pixel centres (RING order).
+__global__ void __launch_bounds__(256) k_hp_centres(int64_t nside, double* centres) {
+  const int64_t npix = 12 * nside * nside;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ir, ip;
+    hp_pix_ring(nside, p, &ir, &ip);
+    double v[3];
+    hp_centre(hp_ring(nside, ir), ip, v);
+    centres[3 * p] = v[0];
+    centres[3 * p + 1] = v[1];
+    centres[3 * p + 2] = v[2];
+  }
+}
 
 // One warp per particle: pass 1 (sums), pass 2 (deposit).
 __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
@@ -227,6 +257,7 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
     dx = sqrt(dx);
     if (dx < h) continue;
     P.dx = dx;
+    P.dxinv = 1.0 / dx;
     P.proj = asin(h / dx);
     P.hinv = 1.0 / P.proj;
     P.scale = 1.0 / ((ang_pix * dx) * (ang_pix * dx));
@@ -263,7 +294,7 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
       for (int64_t k = lo + lane; k <= hi; k += 32) {
         double pc[3], wk, a;
         bool in;
-        hp_centre(R, ((k % R.nr) + R.nr) % R.nr, pc);
+        pixel_centre(H, R, ((k % R.nr) + R.nr) % R.nr, pc);
         hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
         da += a;
         nt += 1;
@@ -317,7 +348,7 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
         double pc[3], wk, a;
         bool in;
         const int64_t kk = ((k % R.nr) + R.nr) % R.nr;
-        hp_centre(R, kk, pc);
+        pixel_centre(H, R, kk, pc);
         hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
         if (P.fallback) wk = 1.0;
         const double pw = P.area_norm * wk * a;
@@ -358,7 +389,8 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
 
 void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtype, int64_t n, const void* pos,
                     const void* hsml, const void* m, const void* rho, const void* q, const void* w,
-                    double* allsky, double* weight, DevStatus* st, int num_sms, cudaStream_t s) {
+                    double* allsky, double* weight, double* centres, bool fill_centres, DevStatus* st,
+                    int num_sms, cudaStream_t s) {
   HpArgs H;
   H.nside = nside;
   H.n = n;
@@ -374,7 +406,9 @@ void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtyp
   H.w = w;
   H.allsky = allsky;
   H.weight = weight;
+  H.centres = centres;
   H.st = st;
+  if (centres && fill_centres) k_hp_centres<<<num_sms * 16, 256, 0, s>>>(nside, centres);
   int64_t grid = (n * 32 + 255) / 256;
   if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
   if (grid < 1) grid = 1;
