@@ -28,6 +28,8 @@ struct sphg_context {
   cudaEvent_t ev[5] = {};               // phase timing events
   double* hp_centres = nullptr;         // HEALPix pixel-centre table of hp_nside
   int64_t hp_nside = 0;
+  double* hp_dist = nullptr;            // HEALPix per-warp distance slices (pass 1 -> pass 2)
+  int hp_dist_per_lane = 0;
 };
 
 namespace {
@@ -188,6 +190,7 @@ int sphg_context_destroy(sphg_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->ws) cudaFree(ctx->ws);
     if (ctx->hp_centres) cudaFree(ctx->hp_centres);
+    if (ctx->hp_dist) cudaFree(ctx->hp_dist);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     for (int k = 0; k < 5; ++k)
@@ -659,9 +662,24 @@ int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n
     }
   }
   double* centres = ctx->hp_nside == ns ? ctx->hp_centres : nullptr;
+  // per-warp slices of pass-1 distances (16384 per warp, 2.5 GB on 152 SMs;
+  // 2048 when that cannot be had): pass 2 reads them instead of
+  // recomputing the dot product and acos
+  if (n > 0 && !ctx->hp_dist) {
+    const size_t warps = (size_t)ctx->num_sms * sphg::kHpCtasPerSm * 8;
+    for (int per_lane : {512, 64}) {
+      if (cudaMalloc(&ctx->hp_dist, warps * 32 * per_lane * sizeof(double)) == cudaSuccess) {
+        ctx->hp_dist_per_lane = per_lane;
+        break;
+      }
+      cudaGetLastError();
+      ctx->hp_dist = nullptr;
+    }
+  }
   if (n > 0)
     sphg::launch_healpix(ns, hp->kernel, hp->kernel_dim, hp->calc_mean, hp->dtype, n, pos, hsml, mass, rho, bin_q,
-                         weights, allsky, weight, centres, fill, ctx->d_status, ctx->num_sms, s);
+                         weights, allsky, weight, centres, fill, ctx->hp_dist, ctx->hp_dist_per_lane,
+                         ctx->d_status, ctx->num_sms, s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

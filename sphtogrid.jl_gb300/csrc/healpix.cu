@@ -175,13 +175,18 @@ struct HpParticle {
 };
 
 // Kernel weight and contributing area of the pixel centred at `pc`.
-__device__ __forceinline__ void hp_terms(int KERN_RT, int kdim, const HpParticle& P, const double pc[3],
-                                         double ang_pix, double* wk, double* a, bool* inside) {
+// Angular distance of the pixel centred at `pc` from the particle's
+// direction: d / |p| as a product with the reciprocal (within an ulp of the
+// quotient; where acos amplifies that, u is near 0 and the kernel flat).
+__device__ __forceinline__ double hp_ddx(const HpParticle& P, const double pc[3]) {
   double d = 0.0;
   for (int c = 0; c < 3; ++c) d += P.p[c] * pc[c];
-  // d / |p| as a product with the reciprocal (within an ulp of the
-  // quotient: where acos amplifies that, u is near 0 and the kernel flat)
-  const double ddx = acos(fmin(d * P.dxinv, 1.0));
+  return acos(fmin(d * P.dxinv, 1.0));
+}
+
+// Kernel weight and contributing area of a pixel at angular distance ddx.
+__device__ __forceinline__ void hp_terms(int KERN_RT, int kdim, const HpParticle& P, double ddx, double ang_pix,
+                                         double* wk, double* a, bool* inside) {
   const double u = ddx * P.hinv;
   *a = fmax(0.0, fmin(ang_pix, fabs(P.proj - (ddx - 0.5 * ang_pix)))) / ang_pix * P.scale;
   *inside = u <= 1.0;
@@ -208,6 +213,8 @@ struct HpArgs {
   const void *pos, *hsml, *m, *rho, *q, *w;  // pos: 3 per particle
   double *allsky, *weight;
   const double* centres;  // pixel-centre unit vectors (3 per pixel), or NULL
+  double* dist;           // per warp: pass 1's angular distances for pass 2, or NULL
+  int dist_per_lane;      // distances kept per lane (the rest are recomputed)
   DevStatus* st;
 };
 
@@ -235,6 +242,42 @@ __global__ void __launch_bounds__(256) k_hp_centres(int64_t nside, double* centr
     centres[3 * p] = v[0];
     centres[3 * p + 1] = v[1];
     centres[3 * p + 2] = v[2];
+  }
+}
+
+// In-ring index of k, which lies within one ring size of [0, nr) (a disc's
+// in-ring range): one add or subtract instead of a 64-bit modulo.
+__device__ __forceinline__ int64_t ring_wrap(int64_t k, int64_t nr) {
+  if (k < 0) k += nr;
+  else if (k >= nr) k -= nr;
+  return (k >= 0 && k < nr) ? k : ((k % nr) + nr) % nr;
+}
+
+// Calls f(R, kk) for the disc's pixels on rings r0..r1, ring by ring, the
+// lanes striding over each ring's range (the same pixels in the same order
+// on every call).  The rings' geometry and ranges are computed 32 at a
+// time, one ring per lane, and broadcast.
+template <class F>
+__device__ __forceinline__ void for_disc_pixels(const HpArgs& H, const HpDisc& D, int64_t r0, int64_t r1, int lane,
+                                                F&& f) {
+  const unsigned full = 0xffffffffu;
+  for (int64_t rb = r0; rb <= r1; rb += 32) {
+    HpRing mine = {0.0, 0, 1, 0};
+    int64_t lo = 1, hi = 0;
+    if (rb + lane <= r1) {
+      mine = hp_ring(H.nside, rb + lane);
+      hp_ring_range(D, mine, rb + lane, &lo, &hi);
+    }
+    const int nrb = r1 - rb + 1 < 32 ? (int)(r1 - rb + 1) : 32;
+    for (int q = 0; q < nrb; ++q) {
+      HpRing R;
+      R.z = __shfl_sync(full, mine.z, q);
+      R.first = __shfl_sync(full, mine.first, q);
+      R.nr = __shfl_sync(full, mine.nr, q);
+      R.shifted = __shfl_sync(full, mine.shifted, q);
+      const int64_t rlo = __shfl_sync(full, lo, q), rhi = __shfl_sync(full, hi, q);
+      for (int64_t k = rlo + lane; k <= rhi; k += 32) f(R, ring_wrap(k, R.nr));
+    }
   }
 }
 
@@ -284,32 +327,34 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
     // rings that can hold disc pixels
     const int64_t r0 = D.north ? 1 : (D.irmin > 1 ? D.irmin : 1);
     const int64_t r1 = D.south ? D.nrings : (D.irmax < D.nrings ? D.irmax : D.nrings);
-    // pass 1
+    // pass 1 (the lane's j-th pixel keeps its distance at dist[j * 32 + lane]
+    // of the warp's slice, for pass 2)
+    double* dist = H.dist ? H.dist + ((((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * H.dist_per_lane) * 32
+                          : nullptr;
     double dw = 0.0, da = 0.0, swk = 0.0;
     long long nd = 0, nt = 0;
-    for (int64_t ir = r0; ir <= r1; ++ir) {
-      const HpRing R = hp_ring(H.nside, ir);
-      int64_t lo, hi;
-      hp_ring_range(D, R, ir, &lo, &hi);
-      for (int64_t k = lo + lane; k <= hi; k += 32) {
-        double pc[3], wk, a;
-        bool in;
-        pixel_centre(H, R, ((k % R.nr) + R.nr) % R.nr, pc);
-        hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
-        da += a;
-        nt += 1;
-        if (in) {
-          dw += wk * a;
-          nd += 1;
-          swk += wk;
-        }
+    int j = 0;
+    for_disc_pixels(H, D, r0, r1, lane, [&](const HpRing& R, int64_t kk) {
+      double pc[3], wk, a;
+      bool in;
+      pixel_centre(H, R, kk, pc);
+      const double ddx = hp_ddx(P, pc);
+      if (dist && j < H.dist_per_lane) dist[(int64_t)j * 32 + lane] = ddx;
+      ++j;
+      hp_terms(H.kernel, H.kdim, P, ddx, ang_pix, &wk, &a, &in);
+      da += a;
+      nt += 1;
+      if (in) {
+        dw += wk * a;
+        nd += 1;
+        swk += wk;
       }
-    }
+    });
     if (!c_in && lane == 0) {
       double pc[3], wk, a;
       bool in;
       hp_centre(hp_ring(H.nside, cir), cip, pc);
-      hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
+      hp_terms(H.kernel, H.kdim, P, hp_ddx(P, pc), ang_pix, &wk, &a, &in);
       da += a;
       nt += 1;
       if (in) {
@@ -338,31 +383,34 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
     const double area = (m / rho) / dz;
     dz /= (ang_pix * dx) * (ang_pix * dx);
     P.area_norm = area / (double)nd * wpp * ld_elem(H.dtype, H.w, i) * dz;
-    // pass 2
+    // pass 2: the same pixels in the same order
     double sa = 0.0;
-    for (int64_t ir = r0; ir <= r1; ++ir) {
-      const HpRing R = hp_ring(H.nside, ir);
-      int64_t lo, hi;
-      hp_ring_range(D, R, ir, &lo, &hi);
-      for (int64_t k = lo + lane; k <= hi; k += 32) {
-        double pc[3], wk, a;
-        bool in;
-        const int64_t kk = ((k % R.nr) + R.nr) % R.nr;
+    j = 0;
+    for_disc_pixels(H, D, r0, r1, lane, [&](const HpRing& R, int64_t kk) {
+      double wk, a;
+      bool in;
+      double ddx;
+      if (dist && j < H.dist_per_lane) {
+        ddx = dist[(int64_t)j * 32 + lane];
+      } else {
+        double pc[3];
         pixel_centre(H, R, kk, pc);
-        hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
-        if (P.fallback) wk = 1.0;
-        const double pw = P.area_norm * wk * a;
-        atomicAdd(&H.allsky[R.first + kk], P.q * pw);
-        atomicAdd(&H.weight[R.first + kk], pw);
-        sa += a;
+        ddx = hp_ddx(P, pc);
       }
-    }
+      ++j;
+      hp_terms(H.kernel, H.kdim, P, ddx, ang_pix, &wk, &a, &in);
+      if (P.fallback) wk = 1.0;
+      const double pw = P.area_norm * wk * a;
+      atomicAdd(&H.allsky[R.first + kk], P.q * pw);
+      atomicAdd(&H.weight[R.first + kk], pw);
+      sa += a;
+    });
     if (!c_in && lane == 0) {
       double pc[3], wk, a;
       bool in;
       const HpRing R = hp_ring(H.nside, cir);
       hp_centre(R, cip, pc);
-      hp_terms(H.kernel, H.kdim, P, pc, ang_pix, &wk, &a, &in);
+      hp_terms(H.kernel, H.kdim, P, hp_ddx(P, pc), ang_pix, &wk, &a, &in);
       if (P.fallback) wk = 1.0;
       const double pw = P.area_norm * wk * a;
       atomicAdd(&H.allsky[cpix], P.q * pw);
@@ -389,8 +437,8 @@ __global__ void __launch_bounds__(256) k_healpix(HpArgs H) {
 
 void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtype, int64_t n, const void* pos,
                     const void* hsml, const void* m, const void* rho, const void* q, const void* w,
-                    double* allsky, double* weight, double* centres, bool fill_centres, DevStatus* st,
-                    int num_sms, cudaStream_t s) {
+                    double* allsky, double* weight, double* centres, bool fill_centres, double* dist,
+                    int dist_per_lane, DevStatus* st, int num_sms, cudaStream_t s) {
   HpArgs H;
   H.nside = nside;
   H.n = n;
@@ -407,10 +455,12 @@ void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtyp
   H.allsky = allsky;
   H.weight = weight;
   H.centres = centres;
+  H.dist = dist;
+  H.dist_per_lane = dist ? dist_per_lane : 0;
   H.st = st;
   if (centres && fill_centres) k_hp_centres<<<num_sms * 16, 256, 0, s>>>(nside, centres);
   int64_t grid = (n * 32 + 255) / 256;
-  if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
+  if (grid > (int64_t)num_sms * kHpCtasPerSm) grid = (int64_t)num_sms * kHpCtasPerSm;
   if (grid < 1) grid = 1;
   k_healpix<<<(unsigned)grid, 256, 0, s>>>(H);
 }

@@ -22,8 +22,10 @@ void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& m
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s);
 void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtype, int64_t n, const void* pos,
                     const void* hsml, const void* m, const void* rho, const void* q, const void* w,
-                    double* allsky, double* weight, double* centres, bool fill_centres, DevStatus* st,
-                    int num_sms, cudaStream_t s);
+                    double* allsky, double* weight, double* centres, bool fill_centres, double* dist,
+                    int dist_per_lane, DevStatus* st, int num_sms, cudaStream_t s);
+// CTAs (of 256 threads, a warp per particle) per SM of the HEALPix deposit.
+constexpr int kHpCtasPerSm = 16;
 cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_per_s);
 void launch_accumulate(const double* part, double* sum, int64_t len, int num_sms, cudaStream_t s);
 void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one, double* out,
