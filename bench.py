@@ -200,7 +200,7 @@ def bench_gpu(args):
     dev = torch.device("cuda", local)
     if args.workload == "healpix":
         import __graft_entry__ as graft
-        out = bench_healpix(graft.load_package(), dev, args.steps, args.warmup)
+        out = bench_healpix(graft.load_package(), dev, args.steps, args.warmup, n=args.healpix_particles)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -680,6 +680,8 @@ def main():
     ap.add_argument("--workload", default="clumps_3d", choices=["clumps_3d", "large_hdr", "healpix"],
                     help="large_hdr: the large-particle projection (2^27 particles, 4096^2), "
                          "FP32C and deterministic against plain FP64 with the error map")
+    ap.add_argument("--healpix-particles", type=int, default=2 ** 20,
+                    help="particles of the all-sky workload (smaller for profiler captures)")
     ap.add_argument("--batched-tuning", default=None,
                     help="tile_x,tile_y,ctas_per_sm,large_cells instead of autotuning")
     args = ap.parse_args()
