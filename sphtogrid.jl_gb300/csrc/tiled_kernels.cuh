@@ -732,11 +732,21 @@ __global__ void __launch_bounds__(256) k_large_finish(TiledArgs A) {
                            ((int64_t)gridDim.x * blockDim.x) >> 5, threadIdx.x & 31);
 }
 
+// v rounded to the nearest int64 (|v| < 2^62) with 32-bit conversions:
+// below 2^31 one rounding conversion; above, v is an integer (24 significant
+// bits) and splits exactly into h 2^31 + r.  Cheaper than the 64-bit
+// conversion where a cell takes many channels (2D), dearer with two (3D).
+__device__ __forceinline__ long long float_to_ll_split(float v) {
+  if (fabsf(v) < 0x1p31f) return (long long)__float2int_rn(v);
+  const int h = __float2int_rz(v * 0x1p-31f);
+  return (long long)h * 2147483648LL + (long long)__float2int_rz(fmaf(-(float)h, 0x1p31f, v));
+}
+
 // Adds one cell value to a tile accumulator (see k_deposit).
-template <bool DET>
+template <bool DET, bool SPLIT = false>
 __device__ __forceinline__ void acc_cell(float* hi, float* lo, unsigned long long* fx, int i, float v) {
   if (DET) {
-    atomicAdd(&fx[i], (unsigned long long)__float2ll_rn(v));
+    atomicAdd(&fx[i], (unsigned long long)(SPLIT ? float_to_ll_split(v) : __float2ll_rn(v)));
   } else {
     acc_twosum(&hi[i], &lo[i], v);
   }
@@ -777,9 +787,9 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 b
     const double pw = wk * ar * cpv;
     if (pw != 0.0) {
       const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
-      acc_cell<DET>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
+      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
       for (int k = 0; k < nq; ++k)
-        acc_cell<DET>(hi, lo, fx, k * TV + li,
+        acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li,
                       __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
     }
   }
@@ -921,11 +931,11 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
     if (u <= 1.0f) {
       const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
       const int li = lbase + (a * TY + b) * TZ + c;
-      acc_cell<DET>(hi, lo, fx, nq * TV + li, gw * cw);
+      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, gw * cw);
 #pragma unroll
       for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
         if (NQ == 0 && k >= nq) break;
-        acc_cell<DET>(hi, lo, fx, k * TV + li, gw * cq[k]);
+        acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li, gw * cq[k]);
       }
     }
   }
