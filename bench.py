@@ -371,7 +371,9 @@ def bench_gpu(args):
                      "kernel": "k_deposit", "peak_source": peaks[1],
                      "algorithmic_bytes_per_launch": dep_bytes},
         "e2e": {"value": deposits / e2e_s, "unit": "deposits/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                "transfer": ("pinned host buffers read and written in place by the kernels over the "
+                             "host link (no staging copies; host wall clock per call)")},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

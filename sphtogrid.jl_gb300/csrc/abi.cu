@@ -268,6 +268,17 @@ int64_t sphg_output_len(const sphg_params* par, const sphg_options* opt, int32_t
 }
 
 namespace {
+// Device address of page-locked (pinned) host memory, or NULL (pageable
+// memory, or not host memory).
+void* mapped_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // sphg_map with an optional position transform (xform: 0 none, 1 axis
 // permutation `perm`, 2 FP64 matrix `rot`; see sphg::DevParticles).
 int map_impl(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
@@ -325,6 +336,18 @@ int map_impl(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   const size_t psz = dtype_size(pt->pos_dtype), asz = dtype_size(pt->attr_dtype);
   const int64_t pos_span = n > 0 ? (n - 1) * pt->pos_stride_p + 2 * pt->pos_stride_c + 1 : 0;
   const int64_t q_span = n > 0 ? (n - 1) * pt->q_stride_p + (int64_t)(nq - 1) * pt->q_stride_k + 1 : 0;
+  // Pinned host buffers on the FP32C path are used in place over the host
+  // link: K1 reads each particle once (and writes the in-place centring
+  // back), the deposit writes each output value once, so the transfers
+  // overlap the kernels instead of preceding and following them.
+  void* zc[7] = {};
+  bool zero_copy = false;
+  if (host && fp32c && n > 0) {
+    const void* hp[7] = {pt->pos, pt->hsml, pt->mass, pt->rho, pt->weights, pt->bin_q, out};
+    zero_copy = true;
+    for (int k = 0; k < 7 && zero_copy; ++k) zero_copy = (zc[k] = mapped_ptr(hp[k])) != nullptr;
+  }
+  const bool staged = host && !zero_copy;  // inputs copied into the workspace, output copied back
 
   sphg::TiledArgs ta;
   std::memset(&ta, 0, sizeof(ta));
@@ -339,7 +362,7 @@ again:
   // workspace layout
   Carve cv;
   size_t o_pos = 0, o_h = 0, o_m = 0, o_r = 0, o_w = 0, o_q = 0, o_out = 0;
-  if (host) {
+  if (staged) {
     o_pos = cv.take(pos_span * psz);
     o_h = cv.take(n * asz);
     o_m = cv.take(n * asz);
@@ -390,7 +413,15 @@ again:
   for (int k = 0; k < 3; ++k) d.perm[k] = perm ? perm[k] : k;
   for (int k = 0; k < 9; ++k) d.rot[k] = rot ? rot[k] : 0.0;
   double* dout = out;
-  if (host) {
+  if (zero_copy) {
+    d.pos = zc[0];
+    d.hsml = zc[1];
+    d.mass = zc[2];
+    d.rho = zc[3];
+    d.w = zc[4];
+    d.q = zc[5];
+    dout = (double*)zc[6];
+  } else if (host) {
     d.pos = ws + o_pos;
     d.hsml = ws + o_h;
     d.mass = ws + o_m;
@@ -513,7 +544,7 @@ again:
     CK(sphg::launch_tiled_fp32(opt->kernel, ta, ctx->num_sms, s, ev, &n_launch));
     if (ev) CK(cudaEventRecord(ev[4], s));
   }
-  if (host) {
+  if (staged) {
     CK(cudaMemcpyAsync(out, dout, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (opt->center == SPHG_CENTER_INPLACE && n > 0)
       CK(cudaMemcpyAsync(pt->pos, d.pos, pos_span * psz, cudaMemcpyDeviceToHost, s));
