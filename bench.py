@@ -198,6 +198,12 @@ def bench_gpu(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload == "differentiable":
+        import __graft_entry__ as graft
+        out = bench_differentiable(graft.load_package(), dev, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     if args.workload == "healpix":
         import __graft_entry__ as graft
         out = bench_healpix(graft.load_package(), dev, args.steps, args.warmup, n=args.healpix_particles)
@@ -551,6 +557,71 @@ def bench_large(pkg, dev, steps, warmup, n=2 ** 27, npix=4096, seed_grid=512):
             "pixels_carrying_weight": int(keep.sum())}
 
 
+DIFF_WORKLOAD = ("differentiable deposition: N=2^20 Float64 particles uniform in the unit cube, hsml "
+                 "lognormal (median 0.01, sigma 0.5) clipped to [0.002, 0.1], m = 1/N, rho uniform in "
+                 "[0.5, 2], Bin_Quant = Weights = rho, 2D-projected to 512^2 with WendlandC4; loss "
+                 "sum((map - target)^2), target the map of a copy with positions jittered by 0.1 hsml "
+                 "and Bin_Quant scaled lognormal sigma 0.1; seed 0")
+
+
+def bench_differentiable(pkg, dev, steps, warmup, cpu_sample=2 ** 16):
+    """The differentiable deposition: forward map, loss and the hand-written
+    adjoint (dL/d positions, hsml, m, rho, weights, Bin_Quant) on the GPU,
+    each timed with CUDA events, for the FP64 and the FP32C forward; the
+    oracle's forward map on the host cores beside it.  The gradients' check
+    against FP64 central differences (256 particles, 1e-4) is
+    tests/test_gpu_adjoint_full.py."""
+    import torch
+    from sphtogrid_gb300 import synth
+    d = synth.differentiable_2d()
+    n, P = d["pos"].shape[1], 512
+    par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+    rng = np.random.default_rng(4)
+    tpos = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).to(dev).T
+    ts = [torch.from_numpy(np.ascontiguousarray(d[k])).to(dev) for k in ("hsml", "mass", "rho", "bin_q", "weights")]
+    with torch.no_grad():
+        jit = tpos + 0.1 * ts[0] * torch.randn(3, n, dtype=torch.float64, device=dev)
+        qj = ts[3] * torch.from_numpy(rng.lognormal(0.0, 0.1, n)).to(dev)
+        target = pkg.sph_map_differentiable(jit, ts[0], ts[1], ts[2], qj, ts[4], param=par,
+                                            kernel=pkg.WendlandC4(2), dimensions=2)
+    stream = torch.cuda.current_stream(dev)
+    out = {"workload": DIFF_WORKLOAD, "particles": n, "npix": P}
+    for name, prec, adj in (("fp64", "fp64", "fp64"), ("fp64_forward_fp32c_adjoint", "fp64", "fp32c"),
+                            ("fp32c", "fp32c", "fp32c")):
+        leaves = [tpos.clone().requires_grad_(True)] + [t.clone().requires_grad_(True) for t in ts]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        fw = bw = 0.0
+        for it in range(warmup + steps):
+            for t in leaves:
+                t.grad = None
+            ev[0].record(stream)
+            img = pkg.sph_map_differentiable(*leaves, param=par, kernel=pkg.WendlandC4(2),
+                                             dimensions=2, precision=prec, adjoint_precision=adj)
+            loss = ((img - target) ** 2).sum()
+            ev[1].record(stream)
+            loss.backward()
+            ev[2].record(stream)
+            torch.cuda.synchronize(dev)
+            if it >= warmup:
+                fw += ev[0].elapsed_time(ev[1])
+                bw += ev[1].elapsed_time(ev[2])
+        out[name] = {"ms_forward_and_loss": fw / steps, "ms_adjoint": bw / steps,
+                     "ms_forward_backward": (fw + bw) / steps}
+    # the oracle's forward map (the reference has no derivatives), host cores
+    O = oracle_module()
+    m_s = min(cpu_sample, n)
+    opar = O.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+    t0 = time.perf_counter()
+    _, info = O.sph_mapping(np.asfortranarray(d["pos"][:, :m_s]).copy(order="F"), d["hsml"][:m_s],
+                            d["mass"][:m_s], d["rho"][:m_s], d["bin_q"][:m_s], d["weights"][:m_s],
+                            param=opar, kernel="wendlandc4", kernel_dim=2, nthreads=os.cpu_count())
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"kind": "port", "cores": os.cpu_count(),
+                           "sample": f"{m_s} of {n} particles, forward map only (no derivatives in the reference)",
+                           "deposits_per_s": info["deposits"] / cpu_s}
+    return out
+
+
 HEALPIX_WORKLOAD = ("all-sky HEALPix map: N=2^20 particles in a shell 2 < r < 6 around the observer "
                     "(directions isotropic), hsml uniform in [0.02, 0.8], m and rho uniform, Cubic, "
                     "Nside=512, FP64, seed 0")
@@ -679,7 +750,8 @@ def main():
                     help="time the batched workload alone (for profiler runs)")
     ap.add_argument("--batched-maps", type=int, default=96,
                     help="maps in the batched workload (smaller for profiler captures)")
-    ap.add_argument("--workload", default="clumps_3d", choices=["clumps_3d", "large_hdr", "healpix"],
+    ap.add_argument("--workload", default="clumps_3d",
+                    choices=["clumps_3d", "large_hdr", "healpix", "differentiable"],
                     help="large_hdr: the large-particle projection (2^27 particles, 4096^2), "
                          "FP32C and deterministic against plain FP64 with the error map")
     ap.add_argument("--healpix-particles", type=int, default=2 ** 20,

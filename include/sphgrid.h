@@ -252,7 +252,11 @@ int sphg_accumulate(sphg_context *ctx, int64_t len, const double *part, double *
  * into `grads`.  Kernel weights are recomputed, not stored.  Particles the
  * forward skips (filtered out, or q == 0 without calc_mean) get zero
  * gradients.  Device memory only; positions must be centred the way the
- * forward saw them (use SPHG_CENTER_READONLY in both, or NONE after INPLACE). */
+ * forward saw them (use SPHG_CENTER_READONLY in both, or NONE after INPLACE).
+ * opt->precision: SPHG_PREC_FP64 (FP64 throughout) or SPHG_PREC_FP32C (per-cell
+ * weights and derivatives in FP32 with compensated sums, the per-particle
+ * finish in FP64; particles the FP32C forward would redo in FP64 are done in
+ * FP64 here too). */
 int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
                  const sphg_particles *parts, const double *raw, const double *grad_out,
                  const sphg_grads *grads, void *stream);

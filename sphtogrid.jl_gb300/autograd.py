@@ -75,7 +75,7 @@ class SPHMapFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, pos, hsml, m, rho, q, w, spec):
-        param, kernel, dims, reduce_image, calc_mean, precision = spec
+        param, kernel, dims, reduce_image, calc_mean, precision, _ = spec
         dev = pos.device
         L = _lib.lib()
         hnd = _lib.default_context(dev.index or 0).handle
@@ -100,7 +100,7 @@ class SPHMapFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gout):
         pos, hsml, m, rho, q, w, raw = ctx.saved_tensors
-        param, kernel, dims, reduce_image, calc_mean, precision = ctx.spec
+        param, kernel, dims, reduce_image, calc_mean, _, precision = ctx.spec
         dev = pos.device
         L = _lib.lib()
         hnd = _lib.default_context(dev.index or 0).handle
@@ -133,10 +133,16 @@ class SPHMapFunction(torch.autograd.Function):
 
 def sph_map_differentiable(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param: MappingParameters,
                            kernel: SPHKernel, dimensions: int = 2, reduce_image: bool = True,
-                           calc_mean: bool = False, precision: str = "fp64"):
+                           calc_mean: bool = False, precision: str = "fp64",
+                           adjoint_precision: str | None = None):
     """``sphMapping`` on CUDA tensors with gradients for every particle input.
-    Returns the reduced map ((P, P, Nq) 2D, (P, P, P) 3D) as a float64 tensor."""
+    Returns the reduced map ((P, P, Nq) 2D, (P, P, P) 3D) as a float64 tensor.
+    ``precision`` is the forward's; ``adjoint_precision`` (default: the same)
+    the backward's: "fp64", or "fp32c" (per-cell terms in FP32 with
+    compensated sums; particles whose sums cancel beyond its rounding bound
+    are redone in FP64)."""
     if Weights is None:
         Weights = Rho
-    spec = (param, kernel, dimensions, reduce_image, calc_mean, precision)
+    spec = (param, kernel, dimensions, reduce_image, calc_mean, precision,
+            precision if adjoint_precision is None else adjoint_precision)
     return SPHMapFunction.apply(Pos, HSML, M, Rho, Bin_Quant, Weights, spec)

@@ -745,6 +745,8 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!par || !opt || !pt || !raw || !grad_out || !gr) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
   if (opt->memspace != SPHG_MEM_DEVICE) return fail(ctx, SPHG_ERR_UNSUPPORTED, "adjoint takes device memory");
+  if (opt->precision != SPHG_PREC_FP64 && opt->precision != SPHG_PREC_FP32C)
+    return fail(ctx, SPHG_ERR_ARG, "unknown precision");
   const int dims = opt->dimensions;
   if (dims != 2 && dims != 3) return fail(ctx, SPHG_ERR_DIMS, "");
   const int nq = pt->n_q;
@@ -778,9 +780,13 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   Carve cv;
   const size_t o_g = cv.take((size_t)PD * (nq + 1) * sizeof(double));
+  // FP32C: the image gradients in FP32 too, for the FP32 per-cell path
+  const bool f32 = opt->precision == SPHG_PREC_FP32C;
+  const size_t o_g32 = f32 ? cv.take((size_t)PD * (nq + 1) * sizeof(float)) : 0;
   if (int st = ensure_ws(ctx, cv.off, s)) return st;
   double* gq = (double*)((char*)ctx->ws + o_g);
   double* gw = gq + (int64_t)nq * PD;
+  float* g32 = f32 ? (float*)((char*)ctx->ws + o_g32) : nullptr;
   sphg::DevParticles d;
   d.n = n;
   d.pos_dtype = pt->pos_dtype;
@@ -814,7 +820,7 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
   const bool raw_out = opt->raw_accumulator || (dims == 2 && opt->return_both_maps);
   CK(sphg::launch_adjoint(opt->kernel, d, mp, raw, grad_out, raw_out ? 1 : 0, opt->reduce_image, gq, gw,
-                          gr->pos, gr->hsml, gr->mass, gr->rho, gr->weights, gr->bin_q, ctx->num_sms, s));
+                          gr->pos, gr->hsml, gr->mass, gr->rho, gr->weights, gr->bin_q, g32, ctx->num_sms, s));
   if (!stream) CK(cudaStreamSynchronize(s));
   ctx->last_error.clear();
   return SPHG_OK;

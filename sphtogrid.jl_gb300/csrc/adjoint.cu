@@ -14,11 +14,19 @@
 //   gamma(x) = dL/dW + sum_k q_k dL/dQ_k,   Gamma = sum_x f gamma  (f = g/S),
 //   dL/dK = Gamma,  dL/dq_k = sum_x pw dL/dQ_k,
 //   dL/dtheta = (K/S) sum_x (gamma - Gamma) dg/dtheta   for theta = x, y, z, h,
-// including the derivative of the renormalisation S.  All in FP64.
+// including the derivative of the renormalisation S.
+//
+// Two precisions: FP64 throughout, or (FP32C) the per-cell weights and
+// derivatives in FP32 with compensated (TwoSum) sums per lane and warp, the
+// per-particle finish in FP64.  The FP32 path redoes in FP64 the particles
+// the forward would (every pixel centre near the kernel edge, or a tiny
+// renormalisation sum), footprints of 2^20 cells or more and maps of more
+// than kAdjQ32 quantities.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
 #include "internal.h"
+#include "tiled.cuh"
 
 namespace sphg {
 
@@ -60,10 +68,43 @@ __device__ __forceinline__ double kshape_du(double u) {
   }
 }
 
-// dL/d(out) -> dL/dQ_k, dL/dW in raw row order (row = i*P + j or i*P^2 + j*P + k).
+// FP32 derivative of the un-normalised kernel shape, u < 1 (kshape_du in
+// FP32, the same polynomials).
+template <int KERN>
+__device__ __forceinline__ float kshape_du_f(float u) {
+  if (u >= 1.0f) return 0.0f;
+  if (KERN == 0) {
+    if (u < 0.5f) return u * fmaf(18.0f, u, -12.0f);
+    const float t = 1.0f - u;
+    return -6.0f * t * t;
+  } else if (KERN == 1) {
+    const float a = 1.0f - u, b = (2.0f / 3.0f) - u, c = (1.0f / 3.0f) - u;
+    const float a2 = a * a, b2 = b * b, c2 = c * c;
+    const float a4 = a2 * a2, b4 = b2 * b2, c4 = c2 * c2;
+    if (u < 1.0f / 3.0f) return fmaf(-75.0f, c4, fmaf(30.0f, b4, -5.0f * a4));
+    if (u < 2.0f / 3.0f) return fmaf(30.0f, b4, -5.0f * a4);
+    return -5.0f * a4;
+  } else if (KERN == 2) {
+    const float t = 1.0f - u, t2 = t * t, t5 = t2 * t2 * t;
+    const float p = fmaf(u, fmaf(35.0f / 3.0f, u, 6.0f), 1.0f);
+    return t5 * fmaf(t, fmaf(70.0f / 3.0f, u, 6.0f), -6.0f * p);
+  } else if (KERN == 3) {
+    const float t = 1.0f - u, t2 = t * t, t4 = t2 * t2, t7 = t4 * t2 * t;
+    const float p = fmaf(u, fmaf(u, fmaf(32.0f, u, 25.0f), 8.0f), 1.0f);
+    return t7 * fmaf(t, fmaf(u, fmaf(96.0f, u, 50.0f), 8.0f), -8.0f * p);
+  } else {
+    const float t = 1.0f - u, t2 = t * t, t4 = t2 * t2, t9 = t4 * t4 * t;
+    const float p = fmaf(u, fmaf(u, fmaf(u, fmaf(429.0f / 5.0f, u, 90.0f), 42.0f), 10.0f), 1.0f);
+    return t9 * fmaf(t, fmaf(u, fmaf(u, fmaf(1716.0f / 5.0f, u, 270.0f), 84.0f), 10.0f), -10.0f * p);
+  }
+}
+
+// dL/d(out) -> dL/dQ_k, dL/dW in raw row order (row = i*P + j or i*P^2 + j*P + k);
+// g32 (FP32 path): the same [nq][PD] then [PD], in FP32.
 __global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ raw, const double* __restrict__ g,
                                                      int dims, int64_t P, int nq, int mode, int reduce,
-                                                     double* __restrict__ gq, double* __restrict__ gw) {
+                                                     double* __restrict__ gq, double* __restrict__ gw,
+                                                     float* __restrict__ g32) {
   const int64_t PD = dims == 2 ? P * P : P * P * P;
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < PD;
        row += (int64_t)gridDim.x * blockDim.x) {
@@ -95,6 +136,10 @@ __global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ r
       }
     }
     gw[row] = dw;
+    if (g32) {
+      for (int c = 0; c < nq; ++c) g32[row + c * PD] = (float)gq[row + c * PD];
+      g32[row + (int64_t)nq * PD] = (float)dw;
+    }
   }
 }
 
@@ -103,12 +148,307 @@ struct AdjArgs {
   DevMapParams mp;
   const double* gq;  // [nq][PD]
   const double* gw;  // [PD]
+  const float* g32;  // FP32 path: gq then gw in FP32, or NULL (FP64 throughout)
   int64_t PD;
   double* d_pos;     // strides of pt.pos
   double *d_hsml, *d_mass, *d_rho, *d_w;
   double* d_q;       // strides of pt.q
   DevStatus* st;
 };
+
+// Maps of at most this many quantities take the FP32 path.
+constexpr int kAdjQ32 = 4;
+
+// One mapped particle in FP64 (the warp's lanes stride over its footprint):
+// grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.
+template <int DIMS, int KERN>
+__device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
+                                  double& dK, double* dqk) {
+  const DevParticles& pt = A.pt;
+  const double L = A.mp.L;
+  const int64_t P = A.mp.P;
+  const int nq = pt.nq;
+  const int64_t iMin = q.lo[0], jMin = q.lo[1], kMin = q.lo[2];
+  const int64_t ni = q.hi[0] - iMin + 1, nj = q.hi[1] - jMin + 1, nk = q.hi[2] - kMin + 1;
+  const int64_t njk = nj * nk, F = ni * njk;
+  const double xs[3] = {q.x, q.y, q.z};
+  const double h = q.hsml;
+  // pass 1: renormalisation sum and branch (as the forward)
+  double s_w = 0.0;
+  for (int64_t f = lane; f < F; f += 32) {
+    const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
+    double u, a;
+    cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &u, &a);
+    if (u <= 1.0) s_w += kshape<KERN, double>(u) * a;
+  }
+  s_w = wsum(s_w);
+  const bool fallback = (s_w == 0.0);
+  // pass 2: recompute g and its derivatives, gather the image gradients
+  double S = 0.0, sgg = 0.0, sgd[4] = {0, 0, 0, 0}, sd[4] = {0, 0, 0, 0}, sq[kMaxQ];
+  for (int k = 0; k < nq; ++k) sq[k] = 0.0;
+  for (int64_t f = lane; f < F; f += 32) {
+    const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
+    const int64_t cell[3] = {iMin + ia, jMin + jb, kMin + kc};
+    double dist[3] = {0, 0, 0}, ov[3] = {1, 1, 1}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
+    for (int d = 0; d < DIMS; ++d) {
+      cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
+      const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
+      const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
+      dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
+      doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
+    }
+    const double A_ = ov[0] * ov[1] * ov[2];
+    double dA[4];
+    dA[3] = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      double rest = 1.0;
+      for (int e = 0; e < 3; ++e)
+        if (e != d) rest *= ov[e];
+      dA[d] = d < DIMS ? dox[d] * rest : 0.0;
+      if (d < DIMS) dA[3] += doh[d] * rest;
+    }
+    const double r2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
+    const double rr = sqrt(r2);
+    const double u = rr / h;
+    double g, dg[4];
+    if (fallback) {
+      g = A_;
+      for (int t = 0; t < 4; ++t) dg[t] = dA[t];
+    } else if (u <= 1.0) {
+      const double s = kshape<KERN, double>(u), sp = kshape_du<KERN>(u);
+      g = s * A_;
+      for (int d = 0; d < 3; ++d) {
+        const double du = (d < DIMS && rr > 0.0) ? dist[d] / (rr * h) : 0.0;
+        dg[d] = sp * du * A_ + s * dA[d];
+      }
+      dg[3] = sp * (-u / h) * A_ + s * dA[3];
+    } else {
+      g = 0.0;
+      dg[0] = dg[1] = dg[2] = dg[3] = 0.0;
+    }
+    const int64_t idx = DIMS == 2 ? cell[0] * P + cell[1] : (cell[0] * P + cell[1]) * P + cell[2];
+    double gam = A.gw[idx];
+    for (int k = 0; k < nq; ++k) {
+      const double gqk = A.gq[k * A.PD + idx];
+      const double qk = q.scalar_zero ? 0.0 : ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk);
+      gam += qk * gqk;
+      sq[k] += g * gqk;
+    }
+    S += g;
+    sgg += gam * g;
+    for (int t = 0; t < 4; ++t) {
+      sgd[t] += gam * dg[t];
+      sd[t] += dg[t];
+    }
+  }
+  S = wsum(S);
+  sgg = wsum(sgg);
+  for (int t = 0; t < 4; ++t) {
+    sgd[t] = wsum(sgd[t]);
+    sd[t] = wsum(sd[t]);
+  }
+  for (int k = 0; k < nq; ++k) sq[k] = wsum(sq[k]);
+  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * L;
+  if (S > 0.0) {
+    const double Gam = sgg / S;
+    dK = Gam;
+    for (int t = 0; t < 4; ++t) grad[t] = K / S * (sgd[t] - Gam * sd[t]);
+    for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
+  }
+}
+
+// A compensated FP32 sum (s, c) reduced over the warp, as FP64.
+__device__ __forceinline__ double comp_total(float s, float c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+    float t, e;
+    two_sum(s, so, t, e);
+    s = t;
+    c = c + co + e;
+  }
+  return (double)s + (double)c;
+}
+
+__device__ __forceinline__ void comp_add(float& s, float& c, float v) {
+  float t, e;
+  two_sum(s, v, t, e);
+  s = t;
+  c += e;
+}
+
+// Overlap, centre offset and overlap derivatives of footprint-local pixel a
+// along one axis, f the particle's offset from the footprint origin.
+__device__ __forceinline__ void axis_terms_f(float f, float h, int a, float& dist, float& ov, float& dox,
+                                             float& doh) {
+  const float fa = (float)a;
+  dist = f - fa - 0.5f;
+  ov = fminf(f + h, fa + 1.0f) - fmaxf(f - h, fa);
+  const bool up = f + h < fa + 1.0f, dn = f - h > fa;
+  dox = (up ? 1.0f : 0.0f) - (dn ? 1.0f : 0.0f);
+  doh = (up ? 1.0f : 0.0f) + (dn ? 1.0f : 0.0f);
+}
+
+// Error estimate of the FP32 path.  The image gradient gam = dL/dW +
+// sum_k q_k dL/dQ_k is formed in FP64 per cell (its parts cancel where q is
+// near the map value) and rounded once.  A per-cell weight or derivative
+// carries a relative rounding error of about kTermEps (a few tens of FP32
+// operations), amplified near the kernel edge, where (1 - u)^k turns the
+// rounding of u into kEdgeEps / (1 - u).  The terms' errors are independent,
+// so a sum's error is estimated as three times the root of the summed
+// squared term errors.  A result is kept when that estimate is within
+// kKeepRel of it (the adjoint's bar is 1e-4); otherwise the particle is
+// redone in FP64.
+constexpr float kTermEps = 5e-7f;
+constexpr float kEdgeEps = 6e-7f;
+constexpr double kKeepRel = 2e-5;
+
+// One mapped particle on the FP32 path; false (nothing written) for the
+// particles it leaves to the FP64 path: those the forward redoes in FP64,
+// and those whose sums cancel so that the FP32 terms' rounding bound exceeds
+// kKeepRel of a result (typically a particle with a near-zero gradient next
+// to pixels of tiny W, where dL/dW is large).
+template <int DIMS, int KERN>
+__device__ bool adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
+                                  double& dK, double* dqk) {
+  const DevParticles& pt = A.pt;
+  const int nq = pt.nq;
+  if (nq > kAdjQ32) return false;
+  const int64_t ni = q.hi[0] - q.lo[0] + 1, nj = q.hi[1] - q.lo[1] + 1, nk = q.hi[2] - q.lo[2] + 1;
+  if (ni * nj * nk >= (1 << 20)) return false;
+  const int F = (int)(ni * nj * nk), njk = (int)(nj * nk), nkk = (int)nk;
+  const float inv_njk = inv_small(njk), inv_nk = inv_small(nkk);
+  // the particle relative to its footprint origin (FP64 -> FP32 once)
+  const float fx = (float)(q.x - (double)q.lo[0]), fy = (float)(q.y - (double)q.lo[1]);
+  const float fz = DIMS == 3 ? (float)(q.z - (double)q.lo[2]) : 0.0f;
+  const float h = (float)q.hsml, hinv = 1.0f / h;
+  double qd[kAdjQ32];
+  for (int k = 0; k < kAdjQ32; ++k)
+    qd[k] = (k < nq && !q.scalar_zero) ? ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) : 0.0;
+  const int64_t P = A.mp.P;
+  const int64_t i0 = q.lo[0], j0 = q.lo[1], k0 = q.lo[2];
+  // the image gradient at a footprint pixel, formed in FP64 (its parts
+  // cancel where q is near the map value) and rounded once
+  auto gamma_at = [&](int64_t idx) {
+    double gm = A.gw[idx];
+    for (int k = 0; k < kAdjQ32; ++k) {
+      if (k >= nq) break;
+      gm += qd[k] * A.gq[k * A.PD + idx];
+    }
+    return (float)gm;
+  };
+  // pass 1: renormalisation sum, the smallest u (the forward's test) and
+  // the weighted mean Gam1 of gam, which pass 2 subtracts from every term
+  float s1 = 0.0f, c1 = 0.0f, umin = 3.0e38f, sG1 = 0.0f, cG1 = 0.0f;
+  for (int f = lane; f < F; f += 32) {
+    const int a = fdiv(f, inv_njk), r = f - a * njk;
+    const int b = fdiv(r, inv_nk), c = r - b * nkk;
+    float dx, ox, t0, t1, dy, oy, dz = 0.0f, oz = 1.0f;
+    axis_terms_f(fx, h, a, dx, ox, t0, t1);
+    axis_terms_f(fy, h, b, dy, oy, t0, t1);
+    if (DIMS == 3) axis_terms_f(fz, h, c, dz, oz, t0, t1);
+    const float u = u_of((dx * dx + dy * dy) + dz * dz, hinv);
+    umin = fminf(umin, u);
+    if (u <= 1.0f) {
+      const float g = kshape_f<KERN>(u) * (ox * oy * oz);
+      comp_add(s1, c1, g);
+      const int64_t idx = DIMS == 2 ? (i0 + a) * P + (j0 + b) : ((i0 + a) * P + (j0 + b)) * P + (k0 + c);
+      comp_add(sG1, cG1, gamma_at(idx) * g);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
+  const double S1 = comp_total(s1, c1);
+  if (ill_conditioned((float)S1, umin)) return false;  // warp-uniform
+  const float Gam1 = (float)(comp_total(sG1, cG1) / S1);
+  // pass 2: g, its derivatives and the image gradients (compensated sums)
+  float aS = 0, cS = 0, aG = 0, cG = 0, agd[4] = {}, cgd[4] = {}, ad[4] = {}, cd[4] = {};
+  float aq[kAdjQ32] = {}, cq[kAdjQ32] = {};
+  // sums of the squared term errors: each sum's rounding estimate
+  float bG = 0, bgd[4] = {}, bd[4] = {}, bq[kAdjQ32] = {};
+  for (int f = lane; f < F; f += 32) {
+    const int a = fdiv(f, inv_njk), r = f - a * njk;
+    const int b = fdiv(r, inv_nk), c = r - b * nkk;
+    float dist[3] = {0.0f, 0.0f, 0.0f}, ov[3] = {1.0f, 1.0f, 1.0f}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
+    axis_terms_f(fx, h, a, dist[0], ov[0], dox[0], doh[0]);
+    axis_terms_f(fy, h, b, dist[1], ov[1], dox[1], doh[1]);
+    if (DIMS == 3) axis_terms_f(fz, h, c, dist[2], ov[2], dox[2], doh[2]);
+    const float u = u_of((dist[0] * dist[0] + dist[1] * dist[1]) + dist[2] * dist[2], hinv);
+    if (!(u <= 1.0f)) continue;  // no weight, no derivative
+    const float A_ = ov[0] * ov[1] * ov[2];
+    float dA[4];
+    dA[0] = dox[0] * ov[1] * ov[2];
+    dA[1] = dox[1] * ov[0] * ov[2];
+    dA[2] = DIMS == 3 ? dox[2] * ov[0] * ov[1] : 0.0f;
+    dA[3] = doh[0] * ov[1] * ov[2] + doh[1] * ov[0] * ov[2] + (DIMS == 3 ? doh[2] * ov[0] * ov[1] : 0.0f);
+    const float s = kshape_f<KERN>(u), sp = kshape_du_f<KERN>(u);
+    const float g = s * A_;
+    const float rr = u * h;  // |d|
+    const float dudr = rr > 0.0f ? sp * A_ / (rr * h) : 0.0f;  // d(s A)/d(dist) per unit offset
+    float dg[4];
+    for (int d = 0; d < 3; ++d) dg[d] = (d < DIMS ? dudr * dist[d] : 0.0f) + s * dA[d];
+    dg[3] = sp * (-u * hinv) * A_ + s * dA[3];
+    const int64_t idx = DIMS == 2 ? (i0 + a) * P + (j0 + b) : ((i0 + a) * P + (j0 + b)) * P + (k0 + c);
+    const float eps = kTermEps + kEdgeEps / fmaxf(1.0f - u, 1e-30f);  // this cell's terms
+    for (int k = 0; k < kAdjQ32; ++k) {
+      if (k >= nq) break;
+      const float gqk = A.g32[k * A.PD + idx];
+      comp_add(aq[k], cq[k], g * gqk);
+      const float eq = eps * g * gqk;
+      bq[k] = fmaf(eq, eq, bq[k]);
+    }
+    const float gam = gamma_at(idx), dgam = gam - Gam1;
+    comp_add(aS, cS, g);
+    comp_add(aG, cG, gam * g);
+    bG = fmaf(eps * gam * g, eps * gam * g, bG);
+    // squared error weight of a term (gam - Gam1) x
+    const float eg = eps * dgam;
+    const float w2 = eg * eg;
+    for (int t = 0; t < 4; ++t) {
+      comp_add(agd[t], cgd[t], dgam * dg[t]);
+      comp_add(ad[t], cd[t], dg[t]);
+      bgd[t] = fmaf(dg[t] * dg[t], w2, bgd[t]);
+      const float ed = eps * dg[t];
+      bd[t] = fmaf(ed, ed, bd[t]);
+    }
+  }
+  const double S = comp_total(aS, cS), sgg = comp_total(aG, cG);
+  double sgd[4], sd[4];
+  for (int t = 0; t < 4; ++t) {
+    sgd[t] = comp_total(agd[t], cgd[t]);
+    sd[t] = comp_total(ad[t], cd[t]);
+  }
+  double sq[kAdjQ32];
+  for (int k = 0; k < kAdjQ32; ++k) sq[k] = comp_total(aq[k], cq[k]);
+  // the rounding estimates: three times the root of the warp sums
+  const double BG = 3.0 * sqrt(wsum((double)bG));
+  double Bgd[4], Bd[4], Bq[kAdjQ32];
+  for (int t = 0; t < 4; ++t) {
+    Bgd[t] = 3.0 * sqrt(wsum((double)bgd[t]));
+    Bd[t] = 3.0 * sqrt(wsum((double)bd[t]));
+  }
+  for (int k = 0; k < kAdjQ32; ++k) Bq[k] = 3.0 * sqrt(wsum((double)bq[k]));
+  if (!(S > 0.0)) return false;
+  const double Gam = sgg / S;
+  const double relG = BG / fabs(sgg);  // relative error of Gam (S is a sum of positive terms)
+  bool keep = !(relG > kKeepRel);  // (0 / 0 when every term is 0: kept)
+  // sum (gam - Gam) dg = sum (gam - Gam1) dg - (Gam - Gam1) sum dg
+  const double dG = Gam - (double)Gam1;
+  double val[4];
+  for (int t = 0; t < 4; ++t) {
+    val[t] = sgd[t] - dG * sd[t];
+    const double err = Bgd[t] + fabs(dG) * Bd[t] + fabs(Gam * sd[t]) * (sgg != 0.0 ? relG : 0.0);
+    if (err > kKeepRel * fabs(val[t])) keep = false;
+  }
+  for (int k = 0; k < nq; ++k)
+    if (Bq[k] > kKeepRel * fabs(sq[k])) keep = false;
+  if (!keep) return false;  // warp-uniform: every value is a warp sum
+  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
+  dK = Gam;
+  for (int t = 0; t < 4; ++t) grad[t] = K / S * val[t];
+  for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
+  return true;
+}
 
 template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256) k_adj_particles(AdjArgs A) {
@@ -117,7 +457,6 @@ __global__ void __launch_bounds__(256) k_adj_particles(AdjArgs A) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const DevParticles& pt = A.pt;
   const double L = A.mp.L;
-  const int64_t P = A.mp.P;
   const int nq = pt.nq;
   for (int64_t p = wid; p < pt.n; p += nw) {
     PrepFP64 q;
@@ -126,93 +465,8 @@ __global__ void __launch_bounds__(256) k_adj_particles(AdjArgs A) {
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
     if (state == kPrepMapped) {
-      const int64_t iMin = q.lo[0], jMin = q.lo[1], kMin = q.lo[2];
-      const int64_t ni = q.hi[0] - iMin + 1, nj = q.hi[1] - jMin + 1, nk = q.hi[2] - kMin + 1;
-      const int64_t njk = nj * nk, F = ni * njk;
-      const double xs[3] = {q.x, q.y, q.z};
-      const double h = q.hsml;
-      // pass 1: renormalisation sum and branch (as the forward)
-      double s_w = 0.0;
-      for (int64_t f = lane; f < F; f += 32) {
-        const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
-        double u, a;
-        cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &u, &a);
-        if (u <= 1.0) s_w += kshape<KERN, double>(u) * a;
-      }
-      s_w = wsum(s_w);
-      const bool fallback = (s_w == 0.0);
-      // pass 2: recompute g and its derivatives, gather the image gradients
-      double S = 0.0, sgg = 0.0, sgd[4] = {0, 0, 0, 0}, sd[4] = {0, 0, 0, 0}, sq[kMaxQ];
-      for (int k = 0; k < nq; ++k) sq[k] = 0.0;
-      for (int64_t f = lane; f < F; f += 32) {
-        const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
-        const int64_t cell[3] = {iMin + ia, jMin + jb, kMin + kc};
-        double dist[3] = {0, 0, 0}, ov[3] = {1, 1, 1}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
-        for (int d = 0; d < DIMS; ++d) {
-          cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
-          const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
-          const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
-          dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
-          doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
-        }
-        const double A_ = ov[0] * ov[1] * ov[2];
-        double dA[4];
-        dA[3] = 0.0;
-        for (int d = 0; d < 3; ++d) {
-          double rest = 1.0;
-          for (int e = 0; e < 3; ++e)
-            if (e != d) rest *= ov[e];
-          dA[d] = d < DIMS ? dox[d] * rest : 0.0;
-          if (d < DIMS) dA[3] += doh[d] * rest;
-        }
-        const double r2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
-        const double rr = sqrt(r2);
-        const double u = rr / h;
-        double g, dg[4];
-        if (fallback) {
-          g = A_;
-          for (int t = 0; t < 4; ++t) dg[t] = dA[t];
-        } else if (u <= 1.0) {
-          const double s = kshape<KERN, double>(u), sp = kshape_du<KERN>(u);
-          g = s * A_;
-          for (int d = 0; d < 3; ++d) {
-            const double du = (d < DIMS && rr > 0.0) ? dist[d] / (rr * h) : 0.0;
-            dg[d] = sp * du * A_ + s * dA[d];
-          }
-          dg[3] = sp * (-u / h) * A_ + s * dA[3];
-        } else {
-          g = 0.0;
-          dg[0] = dg[1] = dg[2] = dg[3] = 0.0;
-        }
-        const int64_t idx = DIMS == 2 ? cell[0] * P + cell[1] : (cell[0] * P + cell[1]) * P + cell[2];
-        double gam = A.gw[idx];
-        for (int k = 0; k < nq; ++k) {
-          const double gqk = A.gq[k * A.PD + idx];
-          const double qk = q.scalar_zero ? 0.0 : ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk);
-          gam += qk * gqk;
-          sq[k] += g * gqk;
-        }
-        S += g;
-        sgg += gam * g;
-        for (int t = 0; t < 4; ++t) {
-          sgd[t] += gam * dg[t];
-          sd[t] += dg[t];
-        }
-      }
-      S = wsum(S);
-      sgg = wsum(sgg);
-      for (int t = 0; t < 4; ++t) {
-        sgd[t] = wsum(sgd[t]);
-        sd[t] = wsum(sd[t]);
-      }
-      for (int k = 0; k < nq; ++k) sq[k] = wsum(sq[k]);
-      const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * L;
-      if (S > 0.0) {
-        const double Gam = sgg / S;
-        dK = Gam;
-        for (int t = 0; t < 4; ++t) grad[t] = K / S * (sgd[t] - Gam * sd[t]);
-        for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
-      }
+      if (!(A.g32 && adj_particle_fp32<DIMS, KERN>(A, p, q, lane, grad, dK, dqk)))
+        adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
     }
     if (lane == 0) {
       // K = w m L^3 / rho (2D), times L in 3D
@@ -246,18 +500,20 @@ void launch_adj_dims(int kernel, const AdjArgs& A, int grid, cudaStream_t s) {
 cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParams& mp, const double* raw,
                            const double* grad_out, int mode, int reduce, double* gq, double* gw,
                            double* d_pos, double* d_hsml, double* d_mass, double* d_rho, double* d_w,
-                           double* d_q, int num_sms, cudaStream_t s) {
+                           double* d_q, float* g32, int num_sms, cudaStream_t s) {
   const int dims = mp.dims;
   const int64_t P = mp.P;
   const int64_t PD = dims == 2 ? P * P : P * P * P;
   int64_t g1 = (PD + 255) / 256;
   if (g1 > num_sms * 8) g1 = num_sms * 8;
-  k_adj_reduce<<<(int)(g1 > 0 ? g1 : 1), 256, 0, s>>>(raw, grad_out, dims, P, pt.nq, mode, reduce, gq, gw);
+  k_adj_reduce<<<(int)(g1 > 0 ? g1 : 1), 256, 0, s>>>(raw, grad_out, dims, P, pt.nq, mode, reduce, gq, gw,
+                                                      g32);
   AdjArgs A;
   A.pt = pt;
   A.mp = mp;
   A.gq = gq;
   A.gw = gw;
+  A.g32 = g32;
   A.PD = PD;
   A.d_pos = d_pos;
   A.d_hsml = d_hsml;

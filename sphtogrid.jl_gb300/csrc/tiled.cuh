@@ -129,6 +129,14 @@ __device__ __forceinline__ void acc_twosum(float* hi, float* lo, float v) {
 }
 
 
+// A record is redone in FP64 when every pixel centre is near or beyond the
+// kernel edge (FP32 cancellation in 1 - u), when its FP32 sum is 0 (the
+// reference's fallback branch) or below 2^-40 (its per-cell factor numerator
+// / S would leave the FP32 range once scaled for the tile accumulators).
+__device__ __forceinline__ bool ill_conditioned(float S, float umin) {
+  return umin > 0.9f || !(S >= 0x1p-40f);
+}
+
 // FP32 kernel shape (no normalisation) via fused multiply-adds.
 template <int KERN>
 __device__ __forceinline__ float kshape_f(float u) {

@@ -350,14 +350,6 @@ __device__ __forceinline__ void store_factor(const TiledArgs& A, int64_t r, doub
   }
 }
 
-// A record is redone in FP64 when every pixel centre is near or beyond the
-// kernel edge (FP32 cancellation in 1 - u), when its FP32 sum is 0 (the
-// reference's fallback branch) or below 2^-40 (its per-cell factor numerator
-// / S would leave the FP32 range once scaled for the tile accumulators).
-__device__ __forceinline__ bool ill_conditioned(float S, float umin) {
-  return umin > 0.9f || !(S >= 0x1p-40f);
-}
-
 // Weight factor of a well-conditioned record from its compensated FP32 sum
 // S + S_err, by the one thread that holds it (weight numerator / S,
 // cic_2D.jl:187-188 and cic_3D.jl:168-169).

@@ -26,7 +26,7 @@ def _case(seed, n, nq=1, hmin=0.02, hmax=0.2, spread=0.5):
     return pos, hsml, m, rho, q, w
 
 
-def _gpu_grads(gpu, case, P, dims, kernel, target_out, precision="fp64"):
+def _gpu_grads(gpu, case, P, dims, kernel, target_out, precision="fp64", adjoint_precision=None):
     pos, hsml, m, rho, q, w = case
     par = gpu.mappingParameters(center=[0.0, 0.0, 0.0], x_size=1.0, y_size=1.0, z_size=1.0,
                                 Npixels=P)
@@ -36,7 +36,7 @@ def _gpu_grads(gpu, case, P, dims, kernel, target_out, precision="fp64"):
           for a in (hsml, m, rho, q, w)]
     out = gpu.sph_map_differentiable(tpos, ts[0], ts[1], ts[2], ts[3], ts[4], param=par,
                                      kernel=gpu.kernel_from_name(kernel, dims), dimensions=dims,
-                                     precision=precision)
+                                     precision=precision, adjoint_precision=adjoint_precision)
     t = torch.tensor(target_out, device=dev)
     flat = out.permute(*reversed(range(out.dim()))).reshape(-1)
     loss = ((flat - t) ** 2).sum()
@@ -56,17 +56,28 @@ def _setup(oracle, case, P, dims, kernel, seed=3):
     return par, raw, out, target
 
 
+@pytest.mark.parametrize("precision,adjoint", [("fp64", "fp64"), ("fp64", "fp32c")])
 @pytest.mark.parametrize("dims,kernel,nq", [(2, "cubic", 1), (2, "wendlandc4", 3),
                                             (2, "quintic", 1), (3, "wendlandc6", 1),
                                             (3, "wendlandc8", 1)])
-def test_adjoint_vs_finite_differences(gpu, oracle, dims, kernel, nq):
+def test_adjoint_vs_finite_differences(gpu, oracle, dims, kernel, nq, precision, adjoint):
+    """FP64 throughout, and the FP32C adjoint (per-cell weights and
+    derivatives in FP32 with compensated sums, FP64 redo where its error
+    estimate exceeds 1e-5) after the FP64 forward.  (After the FP32C forward
+    the adjoint differentiates the FP32C map's loss, which differs from the
+    FP64 loss at pixels of tiny W: test_adjoint_fp32c_forward.)"""
     n, P = (400, 32) if dims == 2 else (150, 16)
     case = _case(dims * 10 + nq, n, nq)
     par, raw, out, target = _setup(oracle, case, P, dims, kernel)
-    grads, out_gpu = _gpu_grads(gpu, case, P, dims, kernel, rows_to_output(target, dims, P))
+    grads, out_gpu = _gpu_grads(gpu, case, P, dims, kernel, rows_to_output(target, dims, P),
+                                precision=precision, adjoint_precision=adjoint)
     # the forward matches the oracle
-    assert np.allclose(out_gpu.reshape(-1, order="F"), rows_to_output(out, dims, P),
-                       rtol=1e-11, atol=1e-13 * np.abs(out).max())
+    ref_out = rows_to_output(out, dims, P)
+    if precision == "fp64":
+        assert np.allclose(out_gpu.reshape(-1, order="F"), ref_out, rtol=1e-11,
+                           atol=1e-13 * np.abs(out).max())
+    else:
+        assert np.abs(out_gpu.reshape(-1, order="F") - ref_out).max() <= 1e-5 * np.abs(ref_out).max()
     parts = np.random.default_rng(1).choice(n, size=24, replace=False)
     for name in PARAMS:
         if dims == 2 and name == "z":
@@ -97,12 +108,15 @@ def test_adjoint_vs_dual_numbers(gpu, oracle, pyoracle):
             assert abs(got - du) <= 1e-6 * abs(du) + 1e-12, (p, name, got, du)
 
 
-def test_adjoint_fallback_and_tiny_particles(gpu, oracle):
-    # sub-pixel particles: g = A in the fallback branch
+@pytest.mark.parametrize("adjoint", ["fp64", "fp32c"])
+def test_adjoint_fallback_and_tiny_particles(gpu, oracle, adjoint):
+    # sub-pixel particles: g = A in the fallback branch (the FP32C adjoint
+    # takes these through its FP64 path, next to FP32 particles)
     dims, kernel, n, P = 2, "cubic", 300, 24
     case = _case(5, n, 1, hmin=0.002, hmax=0.03)
     par, raw, out, target = _setup(oracle, case, P, dims, kernel)
-    grads, _ = _gpu_grads(gpu, case, P, dims, kernel, rows_to_output(target, dims, P))
+    grads, _ = _gpu_grads(gpu, case, P, dims, kernel, rows_to_output(target, dims, P),
+                          adjoint_precision=adjoint)
     for name in ("x", "hsml", "mass", "q"):
         ref = np.array([fd_grad(oracle, case, par, dims, kernel, dims, raw, target, p, name)
                         for p in range(0, n, 10)])
@@ -112,8 +126,8 @@ def test_adjoint_fallback_and_tiny_particles(gpu, oracle):
 
 
 def test_adjoint_fp32c_forward(gpu, oracle):
-    """The differentiable path with the FP32C forward: map within 1e-5 and the
-    FP64 adjoint still within 1e-4 of the finite differences."""
+    """The differentiable path in FP32C (forward and adjoint): map within 1e-5
+    and the adjoint within 1e-4 of the finite differences."""
     dims, kernel, n, P = 2, "wendlandc4", 400, 32
     case = _case(9, n, 1)
     par, raw, out, target = _setup(oracle, case, P, dims, kernel)
