@@ -286,13 +286,17 @@ ChainRulesCore rule of the GPU map (device arrays, `CuArray`s).  The forward
 deposits into the raw accumulator (`raw_accumulator = 1`), reduces it with
 `sphg_reduce`, and keeps the accumulator; the pullback calls `sphg_adjoint`,
 which recomputes the kernel weights instead of storing the particle-pixel
-list and returns dL/d(Pos, HSML, M, Rho, Bin_Quant, Weights).
+list and returns dL/d(Pos, HSML, M, Rho, Bin_Quant, Weights).  `precision`
+is the forward's, `adjoint_precision` (default: the same) the pullback's:
+`:fp64`, or `:fp32c` (per-cell terms in FP32 with compensated sums, particles
+whose sums cancel beyond the FP32 rounding estimate redone in FP64).
 """
 function sphMapping_differentiable end
 
 function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M, Rho, Bin_Quant,
                               Weights; param::mappingParameters, kernel::AbstractSPHKernel,
-                              dimensions::Int=2, reduce_image::Bool=true, precision::Symbol=:fp64)
+                              dimensions::Int=2, reduce_image::Bool=true, precision::Symbol=:fp64,
+                              adjoint_precision::Symbol=precision)
     CUDA = Base.require(Base.PkgId(Base.UUID("052768ef-5323-5732-b1bb-66c8b64840ba"), "CUDA"))
     T = eltype(HSML)
     N = length(M)
@@ -302,8 +306,8 @@ function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M,
     raw = CUDA.zeros(Float64, PD * (nq + 1))
     out = dimensions == 2 ? CUDA.zeros(Float64, P, P, nq) : CUDA.zeros(Float64, P, P, P)
     kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
-    mkopt(raw_acc) = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, false, false,
-                                 precision === :fp32c ? 1 : 0, 0, 2, 1, 0, 0, raw_acc, (0, 0, 0))
+    mkopt(raw_acc, prec=precision) = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, false, false,
+                                                 prec === :fp32c ? 1 : 0, 0, 2, 1, 0, 0, raw_acc, (0, 0, 0))
     ptr(a) = reinterpret(Ptr{Cvoid}, pointer(a))
     pt = SphgParticles(N, dtype_id(eltype(Pos)), dtype_id(T), ptr(Pos), 3, 1, ptr(HSML), ptr(M),
                        ptr(Rho), ptr(Weights), ptr(Bin_Quant), Int32(nq), Int32(0),
@@ -327,7 +331,7 @@ function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M,
         s = ccall((:sphg_adjoint, libsphgrid), Cint,
                   (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles}, Ptr{Cvoid},
                    Ptr{Cvoid}, Ref{SphgGrads}, Ptr{Cvoid}),
-                  context(), SphgParams(param), mkopt(0), pt, ptr(raw), ptr(g), gr, C_NULL)
+                  context(), SphgParams(param), mkopt(0, adjoint_precision), pt, ptr(raw), ptr(g), gr, C_NULL)
         s == 0 || error("sphg_adjoint failed with status $s")
         return (NoTangent(), dpos, dh, dm, dr, dq, dw)
     end
