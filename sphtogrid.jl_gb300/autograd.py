@@ -141,8 +141,12 @@ def sph_map_differentiable(Pos, HSML, M, Rho, Bin_Quant, Weights=None, *, param:
     the backward's: "fp64", or "fp32c" (per-cell terms in FP32 with
     compensated sums; particles whose sums cancel beyond its rounding bound
     are redone in FP64)."""
+    if adjoint_precision is None:
+        adjoint_precision = precision
+    for name, value in (("precision", precision), ("adjoint_precision", adjoint_precision)):
+        if value not in _lib.PREC:
+            raise ValueError(f"{name} must be one of {sorted(_lib.PREC)}, not {value!r}")
     if Weights is None:
         Weights = Rho
-    spec = (param, kernel, dimensions, reduce_image, calc_mean, precision,
-            precision if adjoint_precision is None else adjoint_precision)
+    spec = (param, kernel, dimensions, reduce_image, calc_mean, precision, adjoint_precision)
     return SPHMapFunction.apply(Pos, HSML, M, Rho, Bin_Quant, Weights, spec)

@@ -111,6 +111,21 @@ def test_no_device_is_reported(pkg):
     assert e.value.status == 10
 
 
+def test_differentiable_precision_is_validated(pkg):
+    """An unknown forward or adjoint precision is rejected before any device
+    work."""
+    import torch
+    par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=4)
+    t = torch.ones(1, dtype=torch.float64)
+    pos = torch.full((3, 1), 0.5, dtype=torch.float64)
+    with pytest.raises(ValueError, match="adjoint_precision"):
+        pkg.sph_map_differentiable(pos, t, t, t, t, t, param=par, kernel=pkg.Cubic(2),
+                                   adjoint_precision="fp16")
+    with pytest.raises(ValueError, match="precision"):
+        pkg.sph_map_differentiable(pos, t, t, t, t, t, param=par, kernel=pkg.Cubic(2),
+                                   precision="fp32")
+
+
 def test_kernel_constructors(pkg):
     assert pkg.WendlandC4(2).dim == 2 and pkg.Cubic().dim == 3
     assert pkg.kernel_from_name("wendlandc6", 3).kind == 3
