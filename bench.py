@@ -113,7 +113,7 @@ def load_workload(dtype=np.float32):
 
 def oracle_module():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the checker: only the CPU-baseline leg runs it
+    import oracle  # test infrastructure: only the CPU-baseline leg runs it
     oracle.build()
     return oracle
 

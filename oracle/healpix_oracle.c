@@ -1,7 +1,7 @@
 /* healpix_oracle.c -- TEST INFRASTRUCTURE ONLY: a CPU restatement of
  * SPHtoGrid.jl's all-sky HEALPix deposition (src/healpix_interpolation/
  * main.jl:92-227, pixel_weights.jl:1-139, constributing_pixels.jl:1-22,
- * filter_particles.jl:1-53, shared.jl:1-10), the checker of the GPU path.
+ * filter_particles.jl:1-53, shared.jl:1-10), the oracle of the GPU path.
  *
  * The pixel geometry comes from Healpix.jl (not vendored here): the ring
  * scheme of Gorski et al. 2005 (ApJ 622, 759) -- pix2vec, ang2pix, vec2ang and

@@ -1,7 +1,7 @@
 """ctypes binding of the C oracle (``oracle/sph_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker.  The product never
+and the CPU-baseline leg of ``bench.py`` as the oracle.  The product never
 imports this module.
 
 The oracle restates SPHtoGrid.jl's FP64 ``sphMapping`` path

@@ -5,7 +5,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the pytest suite,
  * `__graft_entry__.smoke()` and the CPU-baseline leg of `bench.py` load it as
- * the checker.  No product code path links, loads or calls it.
+ * the oracle.  No product code path links, loads or calls it.
  *
  * Parity status: the rules restated here are pinned by the reference's own
  * self-contained tests (parameter errors, filter / shift, index bijection,

@@ -10,7 +10,7 @@
 // times contributing area, areas, pixel counts) over the warp; pass 2
 // recomputes each pixel's weight and adds it into the two maps with FP64
 // atomics.  The ring geometry (Gorski et al. 2005) is restated from the
-// published algorithm, as the checker restates it.
+// published algorithm, as the oracle restates it.
 #include <cuda_runtime.h>
 
 #include "common.cuh"

@@ -23,7 +23,7 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def oracle():
-    import oracle as O  # the checker (test infrastructure)
+    import oracle as O  # the oracle (test infrastructure)
     O.build()
     return O
 

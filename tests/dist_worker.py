@@ -1,5 +1,5 @@
 """Rank body of the world-size-2 ``distributed_cic_map`` test: each rank maps
-its sub-files with the oracle (the checker), sums them with a host
+its sub-files with the oracle, sums them with a host
 accumulator and reduces on the host, so the test exercises the sub-file
 assignment and the cross-rank all-reduce without a GPU."""
 import os

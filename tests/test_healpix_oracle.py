@@ -1,4 +1,4 @@
-"""The HEALPix oracle (the checker of the all-sky path): the ring-scheme
+"""The HEALPix oracle (of the all-sky path): the ring-scheme
 pixel functions against the known pixel centres of Gorski et al. 2005 and
 self-consistency, the disc query against a brute-force search over all pixel
 centres, and healpix_map's conservation of the particles' weight."""
