@@ -354,7 +354,11 @@ int map_impl(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   if (fp32c) sphg::tiled_geometry(dims, P, ta.tdim, ta.ntile, &ta.n_tiles);
   int rerun = 0;
   long long pair_cap = (long long)ctx->pair_cap;
-  if (fp32c && pair_cap < 8 * n + ta.n_tiles) pair_cap = 8 * n + ta.n_tiles;
+  // first guess of the (particle, tile) overlaps (64-byte pair records): a
+  // 2D footprint meets about 1.5 tiles, a 3D one 3-7; more re-runs once
+  // with the exact count, which the context keeps
+  const long long guess = (dims == 2 ? 3 : 8) * n + ta.n_tiles;
+  if (fp32c && pair_cap < guess) pair_cap = guess;
   long long chunk_cap = (long long)ctx->chunk_cap;
   if (fp32c && chunk_cap < 4096) chunk_cap = 4096;
 
@@ -377,7 +381,7 @@ again:
   size_t o_acc = 0;
   if (!fp32c) o_acc = cv.take((acc_in_out ? (dims == 3 && !raw_out ? PD : 0) : PD * (nq + 1)) * sizeof(double));
   size_t o_box = 0, o_dim = 0, o_geo = 0, o_cp = 0, o_aux = 0, o_qv = 0, o_cnt = 0, o_start = 0,
-         o_pairs = 0, o_nrec = 0, o_exps = 0, o_large = 0, o_lstart = 0, o_part = 0, o_cpm = 0, o_cpe = 0;
+         o_pairs = 0, o_exps = 0, o_large = 0, o_lstart = 0, o_part = 0, o_cpm = 0, o_cpe = 0;
   const int64_t cap = n > 0 ? n : 1;
   if (fp32c) {
     o_box = cv.take(cap * sizeof(int4));
@@ -388,10 +392,9 @@ again:
     o_cpe = cv.take(cap * sizeof(int));
     o_aux = cv.take(cap * sizeof(double));
     o_qv = cv.take(cap * nq * sizeof(float));
-    o_cnt = cv.take((2 * ta.n_tiles + 2) * sizeof(int));  // counts, fill, record and large counters
+    o_cnt = cv.take(sphg::tiled_counter_ints(ta.n_tiles) * sizeof(int));  // tile counts and fills, record counters
     o_start = cv.take((ta.n_tiles + 1) * sizeof(long long));
-    o_pairs = cv.take(pair_cap * sizeof(int));
-    o_nrec = o_cnt + 2 * ta.n_tiles * sizeof(int);
+    o_pairs = cv.take(pair_cap * sphg::kPairRecBytes);
     o_exps = cv.take((sphg::kMaxQ + 1) * sizeof(int));
     o_large = cv.take(cap * sizeof(int));
     o_lstart = cv.take((cap + 1) * sizeof(long long));
@@ -518,15 +521,12 @@ again:
     ta.cpe = (int*)(ws + o_cpe);
     ta.aux = (double*)(ws + o_aux);
     ta.qv = (float*)(ws + o_qv);
-    ta.tile_count = (int*)(ws + o_cnt);
-    ta.tile_fill = ta.tile_count + ta.n_tiles;
-    ta.n_rec = (int*)(ws + o_nrec);
+    sphg::bind_counters(ta, (int*)(ws + o_cnt));
     ta.tile_start = (long long*)(ws + o_start);
-    ta.pairs = (int*)(ws + o_pairs);
+    ta.prec = (uint4*)(ws + o_pairs);
     ta.pair_cap = pair_cap;
     ta.exps = (int*)(ws + o_exps);
     ta.det = opt->deterministic ? 1 : 0;
-    ta.n_large = ta.n_rec + 1;
     ta.large = (int*)(ws + o_large);
     ta.large_start = (long long*)(ws + o_lstart);
     ta.partials = (float4*)(ws + o_part);
@@ -539,7 +539,7 @@ again:
     ta.mode = raw_out ? 1 : (dims == 3 ? 2 : 0);
     ta.reduce = opt->reduce_image;
     ta.w_is_one = opt->reduce_image ? 0 : 1;
-    CK(cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 2) * sizeof(int), s));
+    CK(cudaMemsetAsync(ta.tile_count, 0, sphg::tiled_counter_ints(ta.n_tiles) * sizeof(int), s));
     CK(cudaMemsetAsync(ta.exps, 0x80, (sphg::kMaxQ + 1) * sizeof(int), s));
     CK(sphg::launch_tiled_fp32(opt->kernel, ta, ctx->num_sms, s, ev, &n_launch));
     if (ev) CK(cudaEventRecord(ev[4], s));

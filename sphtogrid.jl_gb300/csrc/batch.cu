@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(256, 6) kb_deposit(BatchDev B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DepositShared sh;
   __shared__ long long t_sh;
+  deposit_init(sh);
   for (;;) {
     if (threadIdx.x == 0) t_sh = (long long)atomicAdd(B.queue, 1ull);
     __syncthreads();
@@ -303,7 +304,7 @@ int build_plan(sphg_batch* b) {
   std::vector<size_t> cnt_off(nm);
   for (int m = 0; m < nm; ++m) {
     cnt_off[m] = cnt_bytes;
-    cnt_bytes += (2 * b->maps[m].n_tiles + 2) * sizeof(int);
+    cnt_bytes += tiled_counter_ints(b->maps[m].n_tiles) * sizeof(int);
   }
   const size_t o_cnt = take(cnt_bytes);
   const size_t o_exps = take((size_t)nm * (kMaxQ + 1) * sizeof(int));
@@ -326,7 +327,7 @@ int build_plan(sphg_batch* b) {
     o.aux = take(cap * sizeof(double));
     o.qv = take(cap * nq * sizeof(float));
     o.start = take((M.n_tiles + 1) * sizeof(long long));
-    o.pairs = take(M.pair_cap * sizeof(int));
+    o.pairs = take(M.pair_cap * kPairRecBytes);
     o.large = take(cap * sizeof(int));
     o.lstart = take((cap + 1) * sizeof(long long));
     o.part = take(M.chunk_cap * sizeof(float4));
@@ -435,12 +436,9 @@ int build_plan(sphg_batch* b) {
     A.cpe = (int*)(base + o.cpe);
     A.aux = (double*)(base + o.aux);
     A.qv = (float*)(base + o.qv);
-    A.tile_count = (int*)(p.counters + cnt_off[m]);
-    A.tile_fill = A.tile_count + M.n_tiles;
-    A.n_rec = A.tile_fill + M.n_tiles;
-    A.n_large = A.n_rec + 1;
+    bind_counters(A, (int*)(p.counters + cnt_off[m]));
     A.tile_start = (long long*)(base + o.start);
-    A.pairs = (int*)(base + o.pairs);
+    A.prec = (uint4*)(base + o.pairs);
     A.pair_cap = M.pair_cap;
     A.large = (int*)(base + o.large);
     A.large_start = (long long*)(base + o.lstart);
@@ -515,6 +513,7 @@ int run_sized(sphg_batch* b) {
     bool grow = false;
     for (int m = 0; m < nm; ++m) {
       if (b->h_status[m].flags & kFlagNonFinite) return bfail(b, SPHG_ERR_NONFINITE, "map " + std::to_string(m));
+      if (b->h_status[m].flags & kFlagTimeout) return bfail(b, SPHG_ERR_TIMEOUT, "map " + std::to_string(m));
       if (!(b->h_status[m].flags & kFlagOverflow)) continue;
       const TiledArgs& A = b->plan.args[m];
       long long total = 0, chunks = 0;
@@ -661,7 +660,8 @@ int sphg_batch_create(sphg_context* ctx, int32_t n_maps, const sphg_map_desc* de
       const int tdx = dims == 2 ? c.tx : kTile3X, tdy = dims == 2 ? c.ty : kTile3Y, tdz = dims == 2 ? 1 : kTile3Z;
       M.n_tiles = ((P + tdx - 1) / tdx) * ((P + tdy - 1) / tdy) * (dims == 3 ? (P + tdz - 1) / tdz : 1);
       const int64_t n = M.desc.parts.n;
-      if (M.pair_cap < 8 * n + M.n_tiles) M.pair_cap = 8 * n + M.n_tiles;
+      const long long guess = (dims == 2 ? 3 : 8) * n + M.n_tiles;  // overlaps, re-sized by run_sized
+      if (M.pair_cap < guess) M.pair_cap = guess;
       if (M.chunk_cap < 4096) M.chunk_cap = 4096;
     }
     if (int st = sphg::build_plan(b)) return done(st);
@@ -719,6 +719,7 @@ int sphg_batch_wait(sphg_batch* b, sphg_stats* stats) {
   bool overflow = false;
   for (int m = 0; m < nm; ++m) {
     if (b->h_status[m].flags & kFlagNonFinite) return bfail(b, SPHG_ERR_NONFINITE, "map " + std::to_string(m));
+    if (b->h_status[m].flags & kFlagTimeout) return bfail(b, SPHG_ERR_TIMEOUT, "map " + std::to_string(m));
     if (b->h_status[m].flags & kFlagOverflow) overflow = true;
   }
   if (overflow) {  // inputs outgrew the captured lists: grow, re-run, re-capture

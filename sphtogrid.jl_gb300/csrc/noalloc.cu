@@ -7,9 +7,9 @@
 // once a time step has started.  cudaMalloc/cudaFree there either fail or
 // synchronise the device in the middle of the step.  This entry point calls
 // neither (nor any allocating library routine): its scratch -- particle
-// records, tile lists, the (particle, tile) pair list and the status word -- is
-// one file-scope static __device__ array of kNoAllocScratchBytes.  Every GPU
-// that loads the library holds that array until the process exits.
+// records, tile lists, the (particle, tile) pair records and the status word
+// -- is one file-scope static __device__ array of kNoAllocScratchBytes.  Every
+// GPU that loads the library holds that array until the process exits.
 //
 // Compiled with --fmad=false (see tiled_fp32.cu).
 #include <cuda_runtime.h>
@@ -79,6 +79,22 @@ int nfail(int st, const std::string& msg) {
   return st;
 }
 
+// center_particles (filter_shift.jl:6-21) written back into the caller's
+// array, after a map that centred on the fly: the same arithmetic as the
+// mapping's centring (prep_particle_fp64), so the map and the array agree.
+__global__ void __launch_bounds__(256) k_center_inplace(sphg::DevParticles pt, sphg::DevMapParams mp) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pt.n; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int64_t off = p * pt.sp + d * pt.sc;
+      double v = sphg::round_to(pt.pos_dtype, sphg::ld_elem(pt.pos_dtype, pt.pos, off) - mp.cen[d]);
+      if (mp.periodic && fabs(v) > mp.boxsize / 2)
+        v = sphg::round_to(pt.pos_dtype, v > 0 ? v - mp.boxsize / 2 : v + mp.boxsize / 2);
+      sphg::st_elem(pt.pos_dtype, pt.pos, off, v);
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -92,6 +108,8 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   if (opt->precision != SPHG_PREC_FP32C) return nfail(SPHG_ERR_UNSUPPORTED, "maps in FP32C only");
   if (opt->memspace != SPHG_MEM_DEVICE) return nfail(SPHG_ERR_UNSUPPORTED, "takes device memory only");
   if (opt->center < 0 || opt->center > 2) return nfail(SPHG_ERR_ARG, "unknown center mode");
+  for (int r = 0; r < 3; ++r)
+    if (opt->reserved[r]) return nfail(SPHG_ERR_ARG, "reserved option fields must be 0");
   if (opt->kernel < 0 || opt->kernel > 4 || (opt->kernel_dim != 2 && opt->kernel_dim != 3))
     return nfail(SPHG_ERR_ARG, "kernel");
   const int nq = pt->n_q;
@@ -140,19 +158,21 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   const size_t o_geo = take(cap * sizeof(float4)), o_cp = take(cap * sizeof(double));
   const size_t o_cpm = take(cap * sizeof(float)), o_cpe = take(cap * sizeof(int));
   const size_t o_aux = take(cap * sizeof(double)), o_qv = take(cap * nq * sizeof(float));
-  const size_t o_cnt = take((2 * ta.n_tiles + 2) * sizeof(int));
+  const size_t o_cnt = take(tiled_counter_ints(ta.n_tiles) * sizeof(int));
   const size_t o_start = take((ta.n_tiles + 1) * sizeof(long long));
   const size_t o_exps = take((kMaxQ + 1) * sizeof(int));
   const size_t o_large = take(cap * sizeof(int)), o_lstart = take((cap + 1) * sizeof(long long));
-  if (off + al(4096 * sizeof(float4)) + al((size_t)ta.n_tiles * sizeof(int)) > kNoAllocScratchBytes)
+  if (off + al(4096 * sizeof(float4)) + al((size_t)ta.n_tiles * kPairRecBytes) > kNoAllocScratchBytes)
     return nfail(SPHG_ERR_ARG, std::to_string(n) + " particles on a " + std::to_string(P) + "^" +
                                    std::to_string(dims) + " grid exceed the " +
                                    std::to_string(kNoAllocScratchBytes >> 20) +
                                    " MiB no-allocation scratch (use sphg_map)");
+  // the rest: an eighth for the large-footprint chunk partials, the remainder
+  // for the (particle, tile) pair records
   const size_t rest = kNoAllocScratchBytes - off;
   const size_t chunk_bytes = al(std::max<size_t>(4096 * sizeof(float4), rest / 8 / sizeof(float4) * sizeof(float4)));
   const size_t o_part = take(chunk_bytes);
-  const size_t pair_bytes = (kNoAllocScratchBytes - off) / sizeof(int) * sizeof(int);
+  const size_t pair_bytes = (kNoAllocScratchBytes - off) / kPairRecBytes * kPairRecBytes;
   const size_t o_pairs = off;
 
   int dev = 0;
@@ -189,7 +209,12 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   }
   mp.boxsize = par->boxsize;
   mp.periodic = par->periodic;
-  mp.center_mode = opt->center;
+  // in-place centring is applied on the fly and written back only after a
+  // map that succeeded: a call that fails (a full scratch) leaves the
+  // caller's positions as they were, so a retry with the same options
+  // (through sphg_map) centres them once
+  const bool inplace = opt->center == SPHG_CENTER_INPLACE;
+  mp.center_mode = inplace ? SPHG_CENTER_READONLY : opt->center;
   mp.filter = opt->filter;
   mp.calc_mean = dims == 2 ? opt->calc_mean : 0;
   mp.kernel_dim = opt->kernel_dim;
@@ -202,7 +227,6 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   ta.pt = d;
   ta.mp = mp;
   ta.mp_re = mp;
-  if (ta.mp_re.center_mode == SPHG_CENTER_INPLACE) ta.mp_re.center_mode = SPHG_CENTER_NONE;
   ta.kern = opt->kernel;
   ta.large_cells = (int)kLargeCells;
   ta.cap = cap;
@@ -214,13 +238,10 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   ta.cpe = (int*)(ws + o_cpe);
   ta.aux = (double*)(ws + o_aux);
   ta.qv = (float*)(ws + o_qv);
-  ta.tile_count = (int*)(ws + o_cnt);
-  ta.tile_fill = ta.tile_count + ta.n_tiles;
-  ta.n_rec = ta.tile_fill + ta.n_tiles;
-  ta.n_large = ta.n_rec + 1;
+  bind_counters(ta, (int*)(ws + o_cnt));
   ta.tile_start = (long long*)(ws + o_start);
-  ta.pairs = (int*)(ws + o_pairs);
-  ta.pair_cap = (long long)(pair_bytes / sizeof(int));
+  ta.prec = (uint4*)(ws + o_pairs);
+  ta.pair_cap = (long long)(pair_bytes / kPairRecBytes);
   ta.exps = (int*)(ws + o_exps);
   ta.det = opt->deterministic ? 1 : 0;
   ta.large = (int*)(ws + o_large);
@@ -238,9 +259,10 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   // everything that accumulates starts from zero (the scratch keeps the last
   // call's contents)
   cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(DevStatus), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ta.tile_count, 0, (2 * ta.n_tiles + 2) * sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ta.tile_count, 0, tiled_counter_ints(ta.n_tiles) * sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(ta.exps, 0x80, (kMaxQ + 1) * sizeof(int), s);
-  if (e == cudaSuccess) e = launch_tiled_fp32(opt->kernel, ta, slot.num_sms, s, nullptr, nullptr);
+  int n_launch = 0;
+  if (e == cudaSuccess) e = launch_tiled_fp32(opt->kernel, ta, slot.num_sms, s, nullptr, &n_launch);
   DevStatus hs;
   std::memset(&hs, 0, sizeof(hs));
   if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
@@ -257,11 +279,29 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
     stats->grid_mass = hs.grid_mass;
     stats->particle_mass = hs.particle_mass;
     stats->centred = cpar;
-    stats->n_launches = 6;
+    stats->n_launches = n_launch;
+  }
+  const bool full = (hs.flags & kFlagOverflow) && !(hs.flags & kFlagNonFinite);
+  if (inplace && n > 0 && !full) {
+    // the reference centres before it maps (and before it meets a
+    // non-finite value), so a finished map or a non-finite input leaves
+    // the caller's positions centred
+    int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)slot.num_sms * 8);
+    k_center_inplace<<<grid, 256, 0, s>>>(d, mp);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return nfail(SPHG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (stats) stats->n_launches += 1;
   }
   if (hs.flags & kFlagNonFinite) return nfail(SPHG_ERR_NONFINITE, "");
-  if (hs.flags & kFlagOverflow)
-    return nfail(SPHG_ERR_ALLOC, "more (particle, tile) overlaps than the no-allocation scratch holds (use sphg_map)");
+  if (hs.flags & kFlagTimeout) return nfail(SPHG_ERR_TIMEOUT, "");
+  if (full)
+    return nfail(SPHG_ERR_ALLOC,
+                 "more (particle, tile) overlaps than the no-allocation scratch holds (use sphg_map; the "
+                 "positions were left uncentred)");
   sphg::set_thread_error("");
   return SPHG_OK;
 }

@@ -12,12 +12,15 @@
 //                     cic_2D.jl:11-72) in FP32 with compensated lane sums; tiny,
 //                     ill-conditioned particles (no pixel centre well inside the
 //                     kernel) are redone in the reference's FP64 arithmetic.
-//                     Writes each record's index into the lists of its tiles.
-//   K4 k_deposit      one CTA per image tile: every (particle, tile) pair adds
-//                     w(u) A c_p (and q times it) to shared-memory accumulators
-//                     with TwoSum-compensated FP32 atomics; the tile is then
-//                     flushed once, in FP64, straight into the output layout
-//                     (reduce_image_2D/3D fused: reduce_image.jl:8-55).
+//                     Writes one 64-byte pair record per (record, tile) pair
+//                     whose cells can reach the kernel support into the
+//                     tile's slot range.
+//   K4 k_deposit      one CTA per image tile: the tile's pair records are
+//                     staged into shared memory by bulk copies (TMA, one per
+//                     16 records, double-buffered per warp); every pair adds
+//                     w(u) A c_p (and q times it) to shared-memory accumulators;
+//                     the tile is then flushed once, in FP64, straight into the
+//                     output layout (reduce_image_2D/3D fused: reduce_image.jl:8-55).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -44,6 +47,29 @@ constexpr int kScaleTop = 24;
 // paths so that deterministic sums agree bit for bit between them.
 constexpr int kTile3X = 8, kTile3Y = 8, kTile3Z = 8;
 
+// One (record, tile) pair as the deposit consumes it, written once by the
+// renormalisation pass into the tile's slot range: 64 bytes (two DRAM
+// sectors), so a tile's pairs form one contiguous stream that the deposit
+// stages into shared memory with bulk copies.
+//   w[0]  {fx, fy, fz, h}: the record's position offsets from its footprint
+//         start and its smoothing length, pixel units (FP32)
+//   w[1]  {1/h, factor mantissa, factor exponent, pack}; an FP64 pair holds
+//         the record index in place of the exponent
+//   w[2]  {a0, b0, c0, tot}: the start of the pair's cell box, footprint-
+//         local, and the record's whole deposit |numerator| 2^-exponent
+//         (FP32, the deterministic mode's tile bound)
+//   w[3]  {q0, q1, q2, q3}: the quantities (more than four channels: the
+//         record index in w[3].x, the deposit reads them by record)
+// pack: tile-local index of the box start (10 bits), the box sides minus one
+// (5 bits each, x y z) and the FP64 flag.
+constexpr int kPairRecWords = 4;  // uint4 per pair record
+constexpr int kPackFP64 = 1 << 25;
+constexpr size_t kPairRecBytes = kPairRecWords * 16;
+
+// Counter ints of one map: tile_count, tile_fill and tile_fill64 per tile,
+// then the record and large-record counters.
+inline int64_t tiled_counter_ints(int64_t n_tiles) { return 3 * n_tiles + 2; }
+
 struct TiledArgs {
   DevParticles pt;
   DevMapParams mp;
@@ -65,9 +91,10 @@ struct TiledArgs {
                     // K3: |numerator|, the record's total deposit into W
   float* qv;        // quantities, qv[k * cap + r]
   int* tile_count;  // per tile, zeroed before K1
-  int* tile_fill;   // per tile, zeroed before K3
+  int* tile_fill;   // per tile, zeroed before K3: FP32 pairs, from the start of the tile's slots
+  int* tile_fill64; // per tile, zeroed before K3: FP64 pairs, from the end of the tile's slots
   long long* tile_start;  // n_tiles + 1
-  int* pairs;
+  uint4* prec;      // pair records, kPairRecWords uint4 per slot (PairRec)
   long long pair_cap;
   // large records (two-phase renormalisation)
   int* n_large;             // count (device counter)
@@ -93,6 +120,16 @@ struct TiledArgs {
                     // bits in the deterministic mode (one scale per tile)
   int* done;        // chunks finished per tile
 };
+
+// Points A's counters (A.n_tiles set) into `base`, tiled_counter_ints(n_tiles)
+// ints laid out as tile_count, tile_fill, tile_fill64, n_rec, n_large.
+inline void bind_counters(TiledArgs& A, int* base) {
+  A.tile_count = base;
+  A.tile_fill = base + A.n_tiles;
+  A.tile_fill64 = base + 2 * A.n_tiles;
+  A.n_rec = base + 3 * A.n_tiles;
+  A.n_large = A.n_rec + 1;
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;

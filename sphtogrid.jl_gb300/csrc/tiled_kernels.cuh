@@ -218,9 +218,16 @@ __device__ __forceinline__ void cell_term_plane(int kern, float2 pxy, float2 ez,
 
 // Per-warp scratch of the renormalisation pass (one instance per kernel,
 // shared by every specialisation it inlines).
+// Per-warp: the 3D plane table while the warp sums a group's records, then
+// the group's pair sources (PairSrc, five uint4 each) while it writes their
+// pair records.
+union NormWarpShared {
+  float2 plane[kNormPlane];
+  uint4 src[32][5];
+};
 struct NormShared {
   float2 tabs[8][3][kNormTab];
-  float2 plane[8][kNormPlane];
+  NormWarpShared w[8];
 };
 
 // The whole footprint of one record from per-axis tables filled by the warp
@@ -324,9 +331,9 @@ __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& u
 // Stores the finished weight factor cpv of record r (FP64, and as FP32
 // mantissa and exponent for the deposit) in place of its numerator, and
 // raises the channel exponents by the record's largest per-cell weight
-// `bound`.
+// `bound`.  Returns the FP32 mantissa and exponent through cm_out / ce_out.
 __device__ __forceinline__ void store_factor(const TiledArgs& A, int64_t r, double cpv, double bound, int fl,
-                                             int* emax) {
+                                             int* emax, float* cm_out = nullptr, int* ce_out = nullptr) {
   // Dolag renormalisation makes the record's deposits into W sum to the
   // numerator; the deterministic mode bounds its tile sums with it
   A.aux[r] = fabs(A.cp[r]);
@@ -335,6 +342,8 @@ __device__ __forceinline__ void store_factor(const TiledArgs& A, int64_t r, doub
   const float cm = (float)frexp(cpv, &ce);
   A.cpm[r] = cm;
   A.cpe[r] = ce;
+  if (cm_out) *cm_out = cm;
+  if (ce_out) *ce_out = ce;
   if (fl) A.box[r].w = fl;
   int e;
   if (bound > 0.0 && bound < 1e300) {
@@ -354,11 +363,11 @@ __device__ __forceinline__ void store_factor(const TiledArgs& A, int64_t r, doub
 // S + S_err, by the one thread that holds it (weight numerator / S,
 // cic_2D.jl:187-188 and cic_3D.jl:168-169).
 __device__ __forceinline__ void finish_scalar(const TiledArgs& A, int64_t r, float S, float S_err, double& c_gm,
-                                              int* emax) {
+                                              int* emax, float* cm = nullptr, int* ce = nullptr) {
   const double Sd = (double)S + (double)S_err;
   const double cpv = A.cp[r] / Sd;
   c_gm += A.aux[r] * Sd;
-  store_factor(A, r, cpv, fabs(cpv), 0, emax);
+  store_factor(A, r, cpv, fabs(cpv), 0, emax, cm, ce);
 }
 
 // Ill-conditioned record (every pixel centre near or beyond the kernel edge,
@@ -488,23 +497,74 @@ __device__ __forceinline__ void tile_cut(int4 bx, int4 dm, int ox, int oy, int o
   k1[2] = min(dm.z, oz + tz - bx.z);
 }
 
-// Appends record r to the list of the t-th tile of its span, unless `tight`
-// (an FP32 record) and no pixel centre of their intersection can lie within
-// the kernel support.  FP64 records may take the fallback weights, which
-// cover every footprint cell, so they keep every tile.
+// x 2^k for |k| <= 2044 by two exact power-of-two factors (no ldexp call).
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+  const int k1 = k / 2, k2 = k - k1;
+  return x * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+}
+
+// What every pair record of one record repeats (PairRec, tiled.cuh).
+struct PairSrc {
+  int4 bx, dm;      // footprint start {iMin, jMin, kMin, flags} and sides
+  float4 g;         // geometry {x - iMin, y - jMin, z - kMin, h}
+  float hinv;       // 1 / h, as the renormalisation pass forms it
+  float cpm;        // FP32 record: factor mantissa
+  int cpe;          // FP32 record: factor exponent; FP64 record: record index
+  float tot;        // FP32 record: |numerator| * 2^-cpe
+  uint4 q;          // quantities 0-3 (more channels: the record index in q.x)
+  bool tight;       // FP32 record: only tiles and cells the support can reach
+};
+
+// The source of record r's pair records, by the lane that finished it
+// (cm, ce: its FP32 factor; FP64 records read their own from memory).
+__device__ __forceinline__ PairSrc pair_src(const TiledArgs& A, int64_t r, bool tight, float cm, int ce) {
+  PairSrc s;
+  s.bx = A.box[r];
+  s.dm = A.dimv[r];
+  s.g = A.geo[r];
+  s.hinv = 1.0f / s.g.w;
+  s.tight = tight;
+  s.cpm = cm;
+  s.cpe = tight ? ce : (int)r;
+  // |numerator| relative to 2^cpe (|cpm| S: within the FP32 range for every
+  // FP32 record, whatever the units); FP64 records: read from aux
+  s.tot = tight ? (float)scale_pow2(A.aux[r], -ce) : 0.0f;
+  const int nq = A.pt.nq;
+  float qv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  if (nq <= 4)
+    for (int k = 0; k < nq; ++k) qv[k] = A.qv[(int64_t)k * A.cap + r];
+  s.q = make_uint4(nq <= 4 ? __float_as_uint(qv[0]) : (unsigned)r, __float_as_uint(qv[1]), __float_as_uint(qv[2]),
+                   __float_as_uint(qv[3]));
+  return s;
+}
+
+// Writes the pair record of record `src` and the t-th tile of its span into
+// the tile's slot range, unless `tight` (an FP32 record) and no pixel centre
+// of their intersection can lie within the kernel support; an FP32 record's
+// cell box is narrowed to the support's bounding box (support_box).  FP64
+// records may take the fallback weights, which cover every footprint cell,
+// so they keep every tile and cell; their records fill the slot range from
+// its end.
 template <int DIMS>
-__device__ __forceinline__ void tile_entry(const TiledArgs& A, const TileSpan& s, int t, int r, int4 bx, int4 dm,
-                                           bool tight, float4 g) {
+__device__ __forceinline__ void write_pair(const TiledArgs& A, const TileSpan& s, int t, const PairSrc& src) {
   const int ta = t / (s.nty * s.ntz), tb = (t / s.ntz) % s.nty, tc = t % s.ntz;
-  if (tight) {
-    int k0[3], k1[3];
-    tile_cut(bx, dm, (s.tx0 + ta) * A.tdim[0], (s.ty0 + tb) * A.tdim[1], (s.tz0 + tc) * A.tdim[2], A.tdim[0],
-             A.tdim[1], A.tdim[2], k0, k1);
-    if (!support_hits<DIMS>(g, k0, k1)) return;
-  }
+  const int ox = (s.tx0 + ta) * A.tdim[0], oy = (s.ty0 + tb) * A.tdim[1], oz = (s.tz0 + tc) * A.tdim[2];
+  int k0[3], k1[3];
+  tile_cut(src.bx, src.dm, ox, oy, oz, A.tdim[0], A.tdim[1], A.tdim[2], k0, k1);
+  if (src.tight && !support_box<DIMS>(src.g, k0, k1)) return;
   const int64_t tile = ((int64_t)(s.tx0 + ta) * A.ntile[1] + (s.ty0 + tb)) * A.ntile[2] + (s.tz0 + tc);
-  const long long slot = A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1);
-  A.pairs[slot] = r;
+  const int lbase = ((src.bx.x + k0[0] - ox) * A.tdim[1] + (src.bx.y + k0[1] - oy)) * A.tdim[2] +
+                    (src.bx.z + k0[2] - oz);
+  const unsigned pack = (unsigned)lbase | (unsigned)(k1[0] - k0[0] - 1) << 10 | (unsigned)(k1[1] - k0[1] - 1) << 15 |
+                        (unsigned)(k1[2] - k0[2] - 1) << 20 | (src.tight ? 0u : (unsigned)kPackFP64);
+  const long long slot = src.tight ? A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1)
+                                   : A.tile_start[tile + 1] - 1 - atomicAdd(&A.tile_fill64[tile], 1);
+  uint4* w = A.prec + slot * kPairRecWords;
+  w[0] = make_uint4(__float_as_uint(src.g.x), __float_as_uint(src.g.y), __float_as_uint(src.g.z),
+                    __float_as_uint(src.g.w));
+  w[1] = make_uint4(__float_as_uint(src.hinv), __float_as_uint(src.cpm), (unsigned)src.cpe, pack);
+  w[2] = make_uint4((unsigned)k0[0], (unsigned)k0[1], (unsigned)k0[2], __float_as_uint(src.tot));
+  w[3] = src.q;
 }
 
 // Warp-wide channel maxima and sums before lane 0 flushes them.
@@ -518,22 +578,38 @@ __device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int di
   }
 }
 
-// Tile-list entries of a group of 32 records, lane j holding record r_j
-// (`mine`; `tight`: an FP32 record, whose own lane knows it).  The
-// group's (record, tile) entries are spread over the lanes, so a record
-// with many tiles does not hold up the warp.
+__device__ __forceinline__ void src_store(uint4* d, const PairSrc& s) {
+  d[0] = make_uint4((unsigned)s.bx.x, (unsigned)s.bx.y, (unsigned)s.bx.z, s.tight ? 1u : 0u);
+  d[1] = make_uint4((unsigned)s.dm.x, (unsigned)s.dm.y, (unsigned)s.dm.z, (unsigned)s.dm.w);
+  d[2] = make_uint4(__float_as_uint(s.g.x), __float_as_uint(s.g.y), __float_as_uint(s.g.z), __float_as_uint(s.g.w));
+  d[3] = make_uint4(__float_as_uint(s.hinv), __float_as_uint(s.cpm), (unsigned)s.cpe, __float_as_uint(s.tot));
+  d[4] = s.q;
+}
+__device__ __forceinline__ PairSrc src_load(const uint4* d) {
+  PairSrc s;
+  const uint4 a = d[0], b = d[1], g = d[2], f = d[3];
+  s.bx = make_int4((int)a.x, (int)a.y, (int)a.z, 0);
+  s.tight = a.w != 0;
+  s.dm = make_int4((int)b.x, (int)b.y, (int)b.z, (int)b.w);
+  s.g = make_float4(__uint_as_float(g.x), __uint_as_float(g.y), __uint_as_float(g.z), __uint_as_float(g.w));
+  s.hinv = __uint_as_float(f.x);
+  s.cpm = __uint_as_float(f.y);
+  s.cpe = (int)f.z;
+  s.tot = __uint_as_float(f.w);
+  s.q = d[4];
+  return s;
+}
+
+// Pair records of a group of 32 records, lane j holding record j (`mine`)
+// and having put its source into srcs[j].  The group's (record, tile) pairs
+// are spread over the lanes, so a record with many tiles does not hold up
+// the warp.
 template <int DIMS>
-__device__ __forceinline__ void fill_group(const TiledArgs& A, int64_t r, bool mine, bool tight, int lane) {
+__device__ __forceinline__ void fill_group(const TiledArgs& A, bool mine, int4 bx, int4 dm,
+                                           const uint4 (*srcs)[5], int lane) {
   const unsigned full = 0xffffffffu;
-  int4 bx = make_int4(0, 0, 0, 0), dm = make_int4(0, 0, 0, 0);
-  float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   TileSpan sp = {0, 0, 0, 1, 1, 0};
-  if (mine) {
-    bx = A.box[r];
-    dm = A.dimv[r];
-    g = A.geo[r];
-    sp = tile_span(A, bx, dm);
-  }
+  if (mine) sp = tile_span(A, bx, dm);
   int incl = sp.nt;  // inclusive scan of the tile counts
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -557,14 +633,9 @@ __device__ __forceinline__ void fill_group(const TiledArgs& A, int64_t r, bool m
     s.nty = __shfl_sync(full, sp.nty, j);
     s.ntz = __shfl_sync(full, sp.ntz, j);
     const int first = __shfl_sync(full, incl - sp.nt, j);
-    const int4 jb = make_int4(__shfl_sync(full, bx.x, j), __shfl_sync(full, bx.y, j), __shfl_sync(full, bx.z, j), 0);
-    const int4 jd = make_int4(__shfl_sync(full, dm.x, j), __shfl_sync(full, dm.y, j), __shfl_sync(full, dm.z, j), 0);
-    const float4 jg = make_float4(__shfl_sync(full, g.x, j), __shfl_sync(full, g.y, j), __shfl_sync(full, g.z, j),
-                                  __shfl_sync(full, g.w, j));
-    const bool jt = __shfl_sync(full, (int)tight, j) != 0;
-    const int64_t jr = __shfl_sync(full, r, j);
-    if (f < total) tile_entry<DIMS>(A, s, f - first, (int)jr, jb, jd, jt, jg);
+    if (f < total) write_pair<DIMS>(A, s, f - first, src_load(srcs[j]));
   }
+  __syncwarp();  // the sources' shared memory is reused by the next group's sums
 }
 
 // K3 body: the warp `wid` of `nw` takes groups of 32 consecutive records
@@ -572,7 +643,7 @@ __device__ __forceinline__ void fill_group(const TiledArgs& A, int64_t r, bool m
 // record's footprint together; lane j keeps record j's sum, and the 32 lanes
 // then finish their records side by side, so the FP64 division (a small
 // fraction of FP32 throughput on GB300) costs one warp instruction sequence
-// per 32 records.  Each lane also writes its record's tile-list entries.
+// per 32 records.  The warp then writes the group's pair records.
 template <int DIMS, int KERN>
 __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int lane, NormShared& sh) {
   const int nrec = *A.n_rec;
@@ -581,7 +652,8 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
   int emax[kMaxQ + 1];
   for (int c = 0; c <= A.pt.nq; ++c) emax[c] = INT_MIN;
   float2(*tab)[kNormTab] = sh.tabs[(threadIdx.x >> 5) & 7];  // one set per warp of a 256-thread CTA
-  float2* plane = sh.plane[(threadIdx.x >> 5) & 7];
+  float2* plane = sh.w[(threadIdx.x >> 5) & 7].plane;
+  uint4(*srcs)[5] = sh.w[(threadIdx.x >> 5) & 7].src;
   for (int64_t g0 = wid * 32; g0 < nrec; g0 += nw * 32) {
     const int cnt = nrec - g0 < 32 ? (int)(nrec - g0) : 32;
     float my_s = 0.0f, my_c = 0.0f, my_u = 0.0f;
@@ -616,8 +688,21 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
     const bool ill = mine && ill_conditioned(my_s, my_u);
     for (unsigned m = __ballot_sync(0xffffffffu, ill); m; m &= m - 1)
       finish_fp64_warp<DIMS, KERN>(A, g0 + __ffs(m) - 1, lane, c_gm, emax);
-    if (mine && !ill) finish_scalar(A, r, my_s, my_c, c_gm, emax);
-    if (!overflow) fill_group<DIMS>(A, r, mine, !ill, lane);
+    float cm = 0.0f;
+    int ce = 0;
+    if (mine && !ill) finish_scalar(A, r, my_s, my_c, c_gm, emax, &cm, &ce);
+    __syncwarp();  // lane 0's FP64 finishes are read by the records' own lanes
+    if (!overflow) {
+      int4 bx = make_int4(0, 0, 0, 0), dm = bx;
+      if (mine) {
+        const PairSrc src = pair_src(A, r, !ill, cm, ce);
+        bx = src.bx;
+        dm = src.dm;
+        src_store(srcs[lane], src);
+      }
+      __syncwarp();
+      fill_group<DIMS>(A, mine, bx, dm, srcs, lane);
+    }
   }
   flush_stats(A, lane, DIMS, c_gm, emax);
 }
@@ -706,13 +791,11 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
       warp_reduce_comp(s, comp, umin);
       if (ill_conditioned(s, umin)) finish_fp64_warp<DIMS, KERN>(A, r, lane, c_gm, emax);
       else if (lane == 0) finish_scalar(A, r, s, comp, c_gm, emax);
-      __syncwarp();
-      const int4 bx = A.box[r];
-      const int4 dm = A.dimv[r];
-      const TileSpan sp = tile_span(A, bx, dm);
-      const bool tight = (bx.w & kRecFP64) == 0;
-      const float4 g = A.geo[r];
-      for (int t = lane; t < sp.nt; t += 32) tile_entry<DIMS>(A, sp, t, (int)r, bx, dm, tight, g);
+      __syncwarp();  // lane 0 wrote the factor
+      const bool tight = (A.box[r].w & kRecFP64) == 0;
+      const PairSrc src = pair_src(A, r, tight, A.cpm[r], A.cpe[r]);
+      const TileSpan sp = tile_span(A, src.bx, src.dm);
+      for (int t = lane; t < sp.nt; t += 32) write_pair<DIMS>(A, sp, t, src);
     }
   }
   flush_stats(A, lane, DIMS, c_gm, emax);
@@ -753,14 +836,22 @@ __device__ __forceinline__ double cell_value(const float* hi, const float* lo, c
 // K4: one CTA per image tile.  DET selects exact int64 fixed-point tile sums
 // (bitwise reproducible) instead of TwoSum-compensated FP32 (hi, lo) pairs;
 // both use 8 bytes per channel and tile pixel.
-// Deposit of one (ill-conditioned record, tile) pair: per-cell weights in the
-// reference's FP64 arithmetic.  Kept out of line so that its FP64 state does
-// not raise the register demand of the FP32 cell loop.
+
+// Deposit of one FP64 pair (an ill-conditioned record, its pair record's
+// words m = w[1], o = w[2]): per-cell weights in the reference's FP64
+// arithmetic over the pair's whole cell box, lane-strided.  Out of line: its
+// FP64 state stays out of the register budget of the FP32 pair loop.
 template <int DIMS, int KERN, int TY, int TZ, bool DET>
-__device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 bx, int4 dm, int a0, int b0, int c0,
-                                               int nb, int nc, int n, int la, int lb, int lc, int nq, int TV,
+__device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4 m, const uint4 o, int nq, int TV,
                                                float* hi, float* lo, unsigned long long* fx, const double* s_scale,
                                                int lane) {
+  const int r = (int)m.z;
+  const unsigned pack = m.w;
+  const int na = (int)((pack >> 10) & 31u) + 1, nb = (int)((pack >> 15) & 31u) + 1, nc = (int)((pack >> 20) & 31u) + 1;
+  const int lbase = (int)(pack & 1023u);
+  const int n = na * nb * nc;
+  const int4 bx = A.box[r];
+  const int4 dm = A.dimv[r];
   PrepFP64 q;
   prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
   const bool fb = (bx.w & kRecFallback) != 0;
@@ -772,48 +863,97 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, int r, int4 b
     const int c = e - bc * nc;
     const int a = fdiv(bc, inv_nb);
     const int b = bc - a * nb;
-    const int ia = a0 + a, jb = b0 + b, kc = c0 + c;
     double u, ar;
-    cell_fp64<DIMS>(q, bx.x + ia, bx.y + jb, bx.z + kc, &u, &ar);
+    cell_fp64<DIMS>(q, bx.x + (int)o.x + a, bx.y + (int)o.y + b, bx.z + (int)o.z + c, &u, &ar);
     const double wk = fb ? 1.0 : (u <= 1.0 ? shape_d<KERN>(A.kern, u) * q.knorm : 0.0);
     const double pw = wk * ar * cpv;
     if (pw != 0.0) {
-      const int li = ((la + ia) * TY + (lb + jb)) * TZ + (lc + kc);
+      const int li = lbase + (a * TY + b) * TZ + c;
       acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
       for (int k = 0; k < nq; ++k)
         acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li,
-                      __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
+                                 __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
     }
   }
 }
 
+// Pair records per bulk copy into a warp's staging buffer (1 KB).
+constexpr int kStage = 16;
+// Bound on the polls of a bulk copy's completion (each poll may suspend the
+// thread for a while in hardware); a copy of 1 KB completes in microseconds.
+constexpr int kSpinLimit = 1 << 22;
+
 // Per-CTA scratch of the tile deposit besides the accumulators: one
 // instance per kernel, shared by every specialisation the kernel inlines.
-// Pairs a warp prepares together (one lane each) before depositing them.
-constexpr int kPairBatch = 16;
-// Channels whose per-pair factors the header holds (more: recomputed).
-constexpr int kHdrQ = 4;
-
-// One (record, tile) pair as the deposit consumes it: its intersection
-// with the tile, the record's position offsets and FP32 factors.
-struct PairHdr {
-  int a0, b0, c0;  // intersection start, footprint-local
-  int dims;        // na | nb << 8 | nc << 16 | FP64-record flag << 24
-  int lbase;       // tile-local cell of the intersection start
-  int r;           // record
-  float fx, fy, fz, h, hinv, cw;
-  float cq[kHdrQ];
-};
-
 struct DepositShared {
   double scale[kMaxQ + 1];  // 2^shift per channel
   double unscale[kMaxQ + 1];  // 2^-shift per channel, for the flush (exact)
   int shift[kMaxQ + 1];
   double bnd[kMaxQ + 1][8];  // deterministic mode: per-warp tile bounds
   float2 tabs[8][3][32];     // per-warp axis tables of the current pair
-  PairHdr hdr[8][kPairBatch];  // per-warp batch of prepared pairs
+  uint4 stage[8][2][kStage * kPairRecWords];  // per-warp double buffer of pair records
+  unsigned long long bar[8][2];               // mbarriers of the staging buffers
+  unsigned phase[8];         // per warp: bit b, the parity buffer b's barrier waits for next
   int last;                  // split tile: this CTA finished it
 };
+
+// Bulk copies (the non-tensor TMA path) into shared memory, completed on an
+// mbarrier that counts the bytes.
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// Orders this thread's earlier shared-memory accesses (generic proxy: data
+// reads, mbarrier initialisation) before later bulk copies and their
+// completions (async proxy).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// `bytes` a multiple of 16, both addresses 16-byte aligned.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// The whole warp waits for the phase of parity `parity` to complete; false
+// when it has not after kSpinLimit polls (warp-uniform).
+__device__ __forceinline__ bool mbar_wait_warp(unsigned long long* bar, unsigned parity) {
+  for (int it = 0; it < kSpinLimit; ++it)
+    if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
+  return false;
+}
+
+// Once per CTA, before its first tile: each warp's lane 0 initialises the
+// warp's two staging barriers, which then live for the CTA (a barrier that
+// bulk copies have completed on is not initialised again).
+__device__ __forceinline__ void deposit_init(DepositShared& sh) {
+  const int warp = (threadIdx.x >> 5) & 7;
+  if ((threadIdx.x & 31) == 0) {
+    mbar_init(&sh.bar[warp][0], 1);
+    mbar_init(&sh.bar[warp][1], 1);
+    sh.phase[warp] = 0;
+    fence_proxy_async_smem();  // the initialised barriers, as the bulk copies see them
+    fence_mbar_init();
+  }
+  __syncwarp();
+}
 
 // Writes one output pixel (i, j, k) from its W and channel values q(c) in
 // the output's layout (raw accumulator, 3D reduced or 2D reduced).
@@ -856,51 +996,15 @@ __device__ __forceinline__ void flush_cell(const TiledArgs& A, int v, int ox, in
   }
 }
 
-// FP32 factor of channel k of record r: cpm * q * 2^(cpe + shift), with q
-// split into mantissa and exponent so no intermediate leaves the FP32 range
-// (each factor is at most 2^62 / S of its channel's scale).
-__device__ __forceinline__ float channel_factor(const TiledArgs& A, int r, int k, float cpm, int cpe, int shift) {
+// FP32 factor of a channel of quantity q for a record of factor
+// cpm 2^cpe: cpm q 2^(cpe + shift), with q split into mantissa and exponent
+// so no intermediate leaves the FP32 range (each factor is at most 2^62 / S
+// of its channel's scale).
+__device__ __forceinline__ float channel_factor(float q, float cpm, int cpe, int shift) {
   float qm;
   int qe;
-  split_f(A.qv[(int64_t)k * A.cap + r], qm, qe);
+  split_f(q, qm, qe);
   return (cpm * qm) * pow2f(cpe + qe + shift);
-}
-
-// Phase A of the deposit: one lane prepares pair (record r, tile at
-// ox, oy, oz) into `H`.
-template <int DIMS, int NQ, int TX, int TY, int TZ>
-__device__ __forceinline__ void prepare_pair(const TiledArgs& A, int r, int ox, int oy, int oz, int nq,
-                                             const int* s_shift, PairHdr& H) {
-  const int4 bx = A.box[r];
-  const int4 dm = A.dimv[r];
-  int k0[3], k1[3];
-  tile_cut(bx, dm, ox, oy, oz, TX, TY, TZ, k0, k1);
-  const bool fp64 = (bx.w & kRecFP64) != 0;
-  float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (!fp64) {
-    // FP32 record: only the cells that can be inside the kernel support
-    g = A.geo[r];
-    if (!support_box<DIMS>(g, k0, k1)) k1[0] = k0[0];  // none: an empty pair
-  }
-  const int a0 = k0[0], b0 = k0[1], c0 = k0[2];
-  const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
-  H.a0 = a0;
-  H.b0 = b0;
-  H.c0 = c0;
-  H.dims = (k1[0] - a0) | ((k1[1] - b0) << 8) | ((k1[2] - c0) << 16) | (fp64 ? (1 << 24) : 0);
-  H.lbase = ((la + a0) * TY + (lb + b0)) * TZ + (lc + c0);
-  H.r = r;
-  if (fp64) return;
-  H.fx = g.x;
-  H.fy = g.y;
-  H.fz = g.z;
-  H.h = g.w;
-  H.hinv = 1.0f / g.w;
-  const float cpm = A.cpm[r];
-  const int cpe = A.cpe[r];
-  H.cw = cpm * pow2f(cpe + s_shift[nq]);
-  if (NQ > 0 && NQ <= kHdrQ)
-    for (int k = 0; k < NQ; ++k) H.cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
 }
 
 // The cells of one (record, tile) pair: the intersection's n = na nb nc
@@ -933,6 +1037,58 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
   }
 }
 
+// One FP32 pair from its staged record R (PairRec): per-axis tables of its
+// cell box, then its cells.  Uniform across the warp.
+template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
+__device__ __forceinline__ void deposit_pair32(const TiledArgs& A, const uint4* R, int nq, int TV, const int* s_shift,
+                                               float2 (*tab)[32], float* hi, float* lo, unsigned long long* fx,
+                                               int lane) {
+  const uint4 g = R[0], m = R[1], o = R[2];
+  const unsigned pack = m.w;
+  const int na = (int)((pack >> 10) & 31u) + 1, nb = (int)((pack >> 15) & 31u) + 1;
+  const int nc = DIMS == 3 ? (int)((pack >> 20) & 31u) + 1 : 1;
+  const int lbase = (int)(pack & 1023u);
+  const float h = __uint_as_float(g.w), hinv = __uint_as_float(m.x), cpm = __uint_as_float(m.y);
+  const int cpe = (int)m.z;
+  const float cw = cpm * pow2f(cpe + s_shift[nq]);
+  float cq[NQ > 0 ? NQ : kMaxQ];
+  {
+    const uint4 q4 = R[3];
+    const unsigned qa[4] = {q4.x, q4.y, q4.z, q4.w};
+    if (NQ > 0 && NQ <= 4) {
+#pragma unroll
+      for (int k = 0; k < (NQ > 0 && NQ <= 4 ? NQ : 1); ++k)
+        cq[k] = channel_factor(__uint_as_float(qa[k]), cpm, cpe, s_shift[k]);
+    } else {  // channel count known at run time: up to four in the record, more by record index
+      for (int k = 0; k < nq; ++k)
+        cq[k] = channel_factor(nq <= 4 ? __uint_as_float(qa[k & 3]) : A.qv[(int64_t)k * A.cap + (int)q4.x], cpm,
+                               cpe, s_shift[k]);
+    }
+  }
+  for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms; axis by selects
+    const int ax = i < na ? 0 : (i < na + nb ? 1 : 2);
+    const int k = i - (ax == 0 ? 0 : (ax == 1 ? na : na + nb));
+    const int c = k + (int)(ax == 0 ? o.x : (ax == 1 ? o.y : o.z));
+    tab[ax][k] = (DIMS == 2 && ax == 2)
+                     ? make_float2(0.0f, 1.0f)
+                     : axis_sq(__uint_as_float(ax == 0 ? g.x : (ax == 1 ? g.y : g.z)), h, c);
+  }
+  __syncwarp();
+  const int n = na * nb * nc;
+  // a run-time kernel shape is dispatched once per pair, so the cell loop
+  // evaluates a compile-time shape
+#define SPHG_CELLS(K) \
+  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
+  if (KERN >= 0) SPHG_CELLS(KERN >= 0 ? KERN : 0);
+  else if (A.kern == 0) SPHG_CELLS(0);
+  else if (A.kern == 1) SPHG_CELLS(1);
+  else if (A.kern == 2) SPHG_CELLS(2);
+  else if (A.kern == 3) SPHG_CELLS(3);
+  else SPHG_CELLS(4);
+#undef SPHG_CELLS
+  __syncwarp();  // the tables are refilled for the next pair
+}
+
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
 __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_raw, DepositShared& sh,
                              int chunk = 0) {
@@ -949,15 +1105,21 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   // after an overflow of the pair list the lists are incomplete: deposit
-  // nothing (the host grows the list and maps again)
-  const bool overflow = (A.st->flags & kFlagOverflow) != 0;
-  // the list holds the pairs the renormalisation pass kept (tile_fill of
-  // the tile_count slots counted for the whole footprint boxes)
-  const long long p0 = A.tile_start[t], p1 = overflow ? p0 : p0 + A.tile_fill[t];
+  // nothing (the host grows the list and maps again); nor after a staging
+  // copy timed out (the call fails)
+  const bool overflow = (A.st->flags & (kFlagOverflow | kFlagTimeout)) != 0;
+  // the tile's slots hold the pairs the renormalisation pass kept: FP32
+  // pairs from the start, FP64 pairs from the end
+  const long long p0 = A.tile_start[t], pe = A.tile_start[t + 1];
+  const int n32 = overflow ? 0 : A.tile_fill[t], n64 = overflow ? 0 : A.tile_fill64[t];
+  const uint4* rec32 = A.prec + p0 * kPairRecWords;
+  const uint4* rec64 = A.prec + (pe - n64) * kPairRecWords;
   const bool split = A.split > 1;
-  // this CTA's pairs: all of the tile's, or its chunk of them
-  const long long c0 = split ? p0 + (p1 - p0) * chunk / A.split : p0;
-  const long long c1 = split ? p0 + (p1 - p0) * (chunk + 1) / A.split : p1;
+  // this CTA's pairs: all of the tile's, or its chunk of each kind
+  const int f0 = split ? (int)((long long)n32 * chunk / A.split) : 0;
+  const int f1 = split ? (int)((long long)n32 * (chunk + 1) / A.split) : n32;
+  const int d0 = split ? (int)((long long)n64 * chunk / A.split) : 0;
+  const int d1 = split ? (int)((long long)n64 * (chunk + 1) / A.split) : n64;
   // channel scales (powers of two): 2^s_shift as double for the flush
   double* s_scale = sh.scale;
   double* s_unscale = sh.unscale;
@@ -969,11 +1131,19 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     double(*s_bnd)[8] = sh.bnd;
     double bnd[kMaxQ + 1];
     for (int c = 0; c < nch; ++c) bnd[c] = 0.0;
-    for (long long s = p0 + threadIdx.x; s < p1; s += blockDim.x) {
-      const int r = A.pairs[s];
-      const double tot = A.aux[r];
+    for (int s = threadIdx.x; s < n32 + n64; s += blockDim.x) {
+      const uint4* R = s < n32 ? rec32 + (int64_t)s * kPairRecWords : rec64 + (int64_t)(s - n32) * kPairRecWords;
+      const uint4 m = R[1];
+      const uint4 q4 = R[3];
+      const unsigned qa[4] = {q4.x, q4.y, q4.z, q4.w};
+      const bool p64 = (m.w & (unsigned)kPackFP64) != 0;
+      const int r = p64 ? (int)m.z : (int)q4.x;  // the record index, where the record holds it
+      const double tot = p64 ? A.aux[r] : scale_pow2((double)__uint_as_float(R[2].w), (int)m.z);
       bnd[nq] += tot;
-      for (int k = 0; k < nq; ++k) bnd[k] += tot * fabs((double)A.qv[(int64_t)k * A.cap + r]);
+      for (int k = 0; k < nq; ++k) {
+        const float qk = (!p64 && nq <= 4) ? __uint_as_float(qa[k & 3]) : A.qv[(int64_t)k * A.cap + r];
+        bnd[k] += tot * fabs((double)qk);
+      }
     }
     for (int c = 0; c < nch; ++c) {
       const double v = warp_sum_d(bnd[c]);
@@ -1000,68 +1170,55 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     s_unscale[threadIdx.x] = ldexp(1.0, -sh);
   }
   __syncthreads();
-  // per-warp axis tables of the current pair's intersection with the tile
   float2(*tab)[32] = sh.tabs[warp & 7];
-  PairHdr* hdr = sh.hdr[warp & 7];
-  // The warp's pairs are p0 + warp + j * nwarp.  Phase A: each of kPairBatch
-  // lanes prepares one pair of the next batch (their record loads are in
-  // flight together, and the per-pair arithmetic runs once per batch);
-  // phase B: the warp deposits the batch pair by pair from the headers.
-  for (long long sb = c0 + warp; sb < c1; sb += (long long)nwarp * kPairBatch) {
-    const long long sj = sb + (long long)lane * nwarp;
-    if (lane < kPairBatch && sj < c1)
-      prepare_pair<DIMS, NQ, TX, TY, TZ>(A, A.pairs[sj], ox, oy, oz, nq, s_shift, hdr[lane]);
-    __syncwarp();
-    const long long left = (c1 - sb + nwarp - 1) / nwarp;
-    const int cnt = left < kPairBatch ? (int)left : kPairBatch;
-    for (int j = 0; j < cnt; ++j) {
-      const PairHdr& H = hdr[j];
-      const int dims = H.dims;
-      const int na = dims & 0xff, nb = (dims >> 8) & 0xff, nc = (dims >> 16) & 0xff;
-      const int n = na * nb * nc;
-      const int a0 = H.a0, b0 = H.b0, c0 = H.c0;
-      if (n == 0) continue;  // no cell within the kernel support (uniform: H is shared)
-      if (dims & (1 << 24)) {
-        const int r = H.r;
-        const int4 bx = A.box[r];
-        const int4 dm = A.dimv[r];
-        const int la = bx.x - ox, lb = bx.y - oy, lc = DIMS == 3 ? bx.z - oz : 0;
-        deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, r, bx, dm, a0, b0, c0, nb, nc, n, la, lb, lc, nq, TV, hi, lo,
-                                                   fx, s_scale, lane);
-      } else {
-        const float h = H.h, hinv = H.hinv, cw = H.cw;
-        float cq[NQ > 0 ? NQ : kMaxQ];
-        if (NQ > 0 && NQ <= kHdrQ) {
-          for (int k = 0; k < nq; ++k) cq[k] = H.cq[k];
-        } else {  // more channels than the header holds
-          const int r = H.r;
-          const float cpm = A.cpm[r];
-          const int cpe = A.cpe[r];
-          for (int k = 0; k < nq; ++k) cq[k] = channel_factor(A, r, k, cpm, cpe, s_shift[k]);
-        }
-        for (int i = lane; i < na + nb + nc; i += 32) {  // separable per-axis terms; axis by selects
-          const int ax = i < na ? 0 : (i < na + nb ? 1 : 2);
-          const int k = i - (ax == 0 ? 0 : (ax == 1 ? na : na + nb));
-          const int c = k + (ax == 0 ? a0 : (ax == 1 ? b0 : c0));
-          tab[ax][k] = (DIMS == 2 && ax == 2) ? make_float2(0.0f, 1.0f)
-                                              : axis_sq(ax == 0 ? H.fx : (ax == 1 ? H.fy : H.fz), h, c);
-        }
-        __syncwarp();
-        // a run-time kernel shape is dispatched once per pair, so the cell
-        // loop evaluates a compile-time shape
-#define SPHG_CELLS(K) \
-  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, H.lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
-        if (KERN >= 0) SPHG_CELLS(KERN >= 0 ? KERN : 0);
-        else if (A.kern == 0) SPHG_CELLS(0);
-        else if (A.kern == 1) SPHG_CELLS(1);
-        else if (A.kern == 2) SPHG_CELLS(2);
-        else if (A.kern == 3) SPHG_CELLS(3);
-        else SPHG_CELLS(4);
-#undef SPHG_CELLS
+  {
+    // FP32 pairs: warp w takes chunks w, w + nwarp, ... of kStage pair
+    // records, each staged into shared memory by one bulk copy while the
+    // warp deposits the previous chunk (two buffers per warp)
+    uint4* stage[2] = {sh.stage[warp & 7][0], sh.stage[warp & 7][1]};
+    unsigned long long* bar = sh.bar[warp & 7];
+    const int nchunk = (f1 - f0 + kStage - 1) / kStage;
+    auto issue = [&](int c, int b) {
+      if (lane == 0 && c < nchunk) {
+        const int s0 = f0 + c * kStage;
+        const int cnt = f1 - s0 < kStage ? f1 - s0 : kStage;
+        mbar_expect_tx(&bar[b], (unsigned)(cnt * kPairRecBytes));
+        bulk_copy_g2s(stage[b], rec32 + (int64_t)s0 * kPairRecWords, (unsigned)(cnt * kPairRecBytes), &bar[b]);
       }
-      __syncwarp();  // the tables are refilled for the next pair
+    };
+    issue(warp, 0);
+    // bit b: the phase buffer b waits for next (the barriers live for the
+    // CTA, initialised once by deposit_init; every copy of an earlier tile
+    // was waited for)
+    unsigned parity = sh.phase[warp & 7];
+    int b = 0;
+    for (int c = warp; c < nchunk; c += nwarp) {
+      issue(c + nwarp, b ^ 1);  // the other buffer was released at the end of the last round
+      if (!mbar_wait_warp(&bar[b], (parity >> b) & 1u)) {
+        // a bulk copy that never completes: record it, wait (bounded) for
+        // the other buffer's copy in flight, deposit nothing more
+        if (lane == 0) atomicOr(&A.st->flags, kFlagTimeout);
+        if (c + nwarp < nchunk) mbar_wait_warp(&bar[b ^ 1], (parity >> (b ^ 1)) & 1u);
+        break;
+      }
+      parity ^= 1u << b;
+      const int s0 = f0 + c * kStage;
+      const int cnt = f1 - s0 < kStage ? f1 - s0 : kStage;
+      for (int j = 0; j < cnt; ++j)
+        deposit_pair32<DIMS, KERN, NQ, TY, TZ, DET>(A, stage[b] + j * kPairRecWords, nq, TV, s_shift, tab, hi, lo,
+                                                    fx, lane);
+      __syncwarp();
+      if (lane == 0) fence_proxy_async_smem();  // this buffer's reads before its next bulk copy
+      b ^= 1;
     }
-    __syncwarp();  // the headers are refilled for the next batch
+    __syncwarp();
+    if (lane == 0) sh.phase[warp & 7] = parity;
+  }
+  // FP64 pairs (ill-conditioned records), warp per pair
+  for (int j = d0 + warp; j < d1; j += nwarp) {
+    const uint4* R = rec64 + (int64_t)j * kPairRecWords;
+    deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, R[1], R[2], nq, TV, hi, lo, fx, s_scale, lane);
+    __syncwarp();
   }
   __syncthreads();
   const int64_t P = A.mp.P;
@@ -1119,24 +1276,31 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
-// Launch bounds by measurement: six CTAs per SM (40 registers).  Eight (32
-// registers) spill the per-pair support narrowing and cell loop to local
-// memory; five leave too few warps to hide the shared-memory latency.
-__global__ void __launch_bounds__(256, 6) k_deposit(TiledArgs A) {
+// Launch bounds: five CTAs per SM (48 registers); at six (40 registers) the
+// pair loop spills to local memory.
+__global__ void __launch_bounds__(256, 5) k_deposit(TiledArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ DepositShared sh;
+  deposit_init(sh);
   deposit_tile<DIMS, KERN, NQ, TX, TY, TZ, DET>(A, blockIdx.x, smem_raw, sh);
 }
 
 template <int DIMS, int KERN, int NQ, bool DET>
 void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
+  // the tile accumulators are dynamic shared memory beside DepositShared;
+  // above the default 48 KB in all the kernel opts in
   if (DIMS == 2) {
     constexpr int TX = 16, TY = 16;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
+    if (sm + sizeof(DepositShared) > 48 * 1024)
+      cudaFuncSetAttribute(k_deposit<2, KERN, NQ, TX, TY, 1, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   } else {
     constexpr int TX = kTile3X, TY = kTile3Y, TZ = kTile3Z;
     const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
+    if (sm + sizeof(DepositShared) > 48 * 1024)
+      cudaFuncSetAttribute(k_deposit<3, KERN, NQ, TX, TY, TZ, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
     k_deposit<3, KERN, NQ, TX, TY, TZ, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   }
 }
