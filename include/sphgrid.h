@@ -270,6 +270,20 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
  * deposit rate.  Synchronous; allocates a few bytes of device memory. */
 int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);
 
+/* Per-particle state and integer pixel ranges, from the device code every
+ * map runs (center_particles and filter_particles_in_image,
+ * filter_shift.jl:6-58; the quantity skip, cic_2D.jl:154-168;
+ * get_xyz and pix_index_min_max, cic_shared.jl:46-52 and :85-99), for
+ * checking them against a reference bit for bit.  state[p]: 0 filtered out,
+ * 1 skipped (every quantity zero without calc_mean), 2 mapped, 3 non-finite
+ * range (the call returns SPHG_ERR_NONFINITE).  ranges[6 p .. 6 p + 5] =
+ * {iMin, iMax, jMin, jMax, kMin, kMax} of a mapped particle (zeros
+ * otherwise; the third axis is 0 0 in 2D; an empty range has max = min - 1).
+ * Device memory only; the positions are read, never written
+ * (SPHG_CENTER_INPLACE is taken as READONLY).  Synchronous. */
+int sphg_footprints(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
+                    const sphg_particles *parts, int64_t *ranges, int8_t *state, void *stream);
+
 /* ------------------------------------------------------- no-allocation map
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory: code running inside a host application that owns all device memory

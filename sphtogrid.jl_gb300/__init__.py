@@ -9,7 +9,7 @@ and the SPHKernels kernel constructors ``Cubic``, ``Quintic``,
 from ._lib import SPHtoGridError, Context, default_context  # noqa: F401
 from .parameters import (Cubic, MappingParameters, Quintic, SPHKernel, WendlandC4,  # noqa: F401
                          WendlandC6, WendlandC8, kernel_from_name, mappingParameters)
-from .mapping import map_it, rotation_matrix_xyz, sphMapping  # noqa: F401
+from .mapping import map_it, rotation_matrix_xyz, sph_footprints, sphMapping  # noqa: F401
 
 
 def __getattr__(name):
@@ -32,6 +32,6 @@ def __getattr__(name):
         return getattr(batch, name)
     raise AttributeError(name)
 
-__all__ = ["mappingParameters", "MappingParameters", "sphMapping", "map_it", "Cubic", "Quintic",
+__all__ = ["mappingParameters", "MappingParameters", "sphMapping", "map_it", "sph_footprints", "Cubic", "Quintic",
            "WendlandC4", "WendlandC6", "WendlandC8", "SPHKernel", "kernel_from_name",
            "SPHtoGridError", "Context", "default_context"]

@@ -193,6 +193,9 @@ def lib():
         L.sphg_probe_smem_rate.restype = i32
         L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]
         L.sphg_accumulate.restype = i32
+        L.sphg_footprints.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),
+                                      C.POINTER(SphgParticles), vp, vp, vp]
+        L.sphg_footprints.restype = i32
         _lib = L
     return _lib
 

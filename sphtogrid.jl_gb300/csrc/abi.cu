@@ -626,6 +626,84 @@ int sphg_map_projected(sphg_context* ctx, const sphg_params* par, const sphg_opt
   return map_impl(ctx, &rp, &o, pt, 1, perm, nullptr, out, stream, stats);
 }
 
+int sphg_footprints(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, const sphg_particles* pt,
+                    int64_t* ranges, int8_t* state, void* stream) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!par || !opt || !pt || (pt->n > 0 && (!ranges || !state))) return fail(ctx, SPHG_ERR_ARG, "NULL argument");
+  const int dims = opt->dimensions;
+  if (dims != 2 && dims != 3) return fail(ctx, SPHG_ERR_DIMS, "");
+  const int nq = pt->n_q;
+  if (nq < 1 || nq > sphg::kMaxQ) return fail(ctx, SPHG_ERR_ARG, "n_q must be in 1..16");
+  if (opt->center < 0 || opt->center > 2) return fail(ctx, SPHG_ERR_ARG, "unknown center mode");
+  if (opt->memspace != SPHG_MEM_DEVICE) return fail(ctx, SPHG_ERR_UNSUPPORTED, "footprints take device memory");
+  if (!valid_dtype(pt->pos_dtype) || !valid_dtype(pt->attr_dtype)) return fail(ctx, SPHG_ERR_ARG, "dtype");
+  const int64_t n = pt->n;
+  if (n < 0) return fail(ctx, SPHG_ERR_ARG, "negative particle count");
+  if (n > 0 && (!pt->pos || !pt->hsml || !pt->bin_q)) return fail(ctx, SPHG_ERR_ARG, "NULL particle array");
+  if (pt->pos_stride_p < 0 || pt->pos_stride_c < 0 || pt->q_stride_p < 0 || pt->q_stride_k < 0)
+    return fail(ctx, SPHG_ERR_ARG, "negative stride");
+  const int64_t P = par->Npixels[0];
+  if (P < 1 || P > (int64_t)1 << 20 || (dims == 3 && P > 4096)) return fail(ctx, SPHG_ERR_ARG, "Npixels out of range");
+  sphg_params cpar;  // centred parameters, as sphg_map derives them
+  {
+    const double* cen = par->center;
+    const double xl[2] = {par->x_lim[0] - cen[0], par->x_lim[1] - cen[0]};
+    const double yl[2] = {par->y_lim[0] - cen[1], par->y_lim[1] - cen[1]};
+    const double zl[2] = {par->z_lim[0] - cen[2], par->z_lim[1] - cen[2]};
+    const double c0[3] = {0.0, 0.0, 0.0};
+    int64_t Pmax = par->Npixels[0];
+    if (par->Npixels[1] > Pmax) Pmax = par->Npixels[1];
+    if (par->Npixels[2] > Pmax) Pmax = par->Npixels[2];
+    int st = sphg_mapping_parameters(xl, yl, zl, c0, -1.0, -1.0, -1.0, -1.0, Pmax, par->boxsize, &cpar);
+    if (st) return fail(ctx, st, g_error);
+  }
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  sphg::DevParticles d;
+  d.n = n;
+  d.pos_dtype = pt->pos_dtype;
+  d.attr_dtype = pt->attr_dtype;
+  d.pos = pt->pos;
+  d.sp = pt->pos_stride_p;
+  d.sc = pt->pos_stride_c;
+  d.hsml = pt->hsml;
+  d.mass = pt->mass;
+  d.rho = pt->rho;
+  d.w = pt->weights;
+  d.q = pt->bin_q;
+  d.nq = nq;
+  d.qsp = pt->q_stride_p;
+  d.qsk = pt->q_stride_k;
+  sphg::DevMapParams mp;
+  for (int k = 0; k < 3; ++k) {
+    mp.cen[k] = par->center[k];
+    mp.lo[k] = cpar.center[k] - cpar.halfsize[k];
+    mp.hi[k] = cpar.center[k] + cpar.halfsize[k];
+  }
+  mp.boxsize = par->boxsize;
+  mp.periodic = par->periodic;
+  // the positions are read, never written
+  mp.center_mode = opt->center == SPHG_CENTER_INPLACE ? SPHG_CENTER_READONLY : opt->center;
+  mp.filter = opt->filter;
+  mp.calc_mean = dims == 2 ? opt->calc_mean : 0;
+  mp.kernel_dim = opt->kernel_dim;
+  mp.dims = dims;
+  mp.L = cpar.len2pix;
+  mp.P = P;
+  mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
+  CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
+  if (n > 0) {
+    sphg::launch_footprints(d, mp, (long long*)ranges, (signed char*)state, ctx->d_status, ctx->num_sms, s);
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(sphg::DevStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (ctx->h_status->flags & sphg::kFlagNonFinite) return fail(ctx, SPHG_ERR_NONFINITE, "");
+  ctx->last_error.clear();
+  return SPHG_OK;
+}
+
 int sphg_reduce(sphg_context* ctx, const sphg_params* par, const sphg_options* opt, int32_t n_q,
                 const double* raw, double* out, void* stream) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");

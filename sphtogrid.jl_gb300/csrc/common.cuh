@@ -157,7 +157,8 @@ struct PrepFP64 {
   bool scalar_zero;
 };
 
-enum { kPrepSkip = 0, kPrepMapped = 1, kPrepNonFinite = 2 };
+// kPrepSkip: filtered out; kPrepZeroQ: every quantity zero without calc_mean.
+enum { kPrepSkip = 0, kPrepMapped = 1, kPrepNonFinite = 2, kPrepZeroQ = 3 };
 
 // center_particles / filter (filter_shift.jl:6-58), the quantity skip
 // (cic_2D.jl:154-168), get_quantities_2D/3D (cic_2D.jl:80-91,
@@ -197,7 +198,7 @@ __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const 
   bool allzero = true;
   for (int k = 0; k < pt.nq; ++k)
     if (ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) != 0.0) allzero = false;
-  if (allzero && !mp.calc_mean) return kPrepSkip;
+  if (allzero && !mp.calc_mean) return kPrepZeroQ;
   o->scalar_zero = (pt.nq > 1) && allzero;
   const double L = mp.L;
   const int64_t P = mp.P;

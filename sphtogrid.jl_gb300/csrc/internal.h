@@ -19,6 +19,8 @@ cudaError_t probe_kernel_image(cudaFuncAttributes* fa);
 
 void launch_plain_fp64(int kernel, const DevParticles& pt, const DevMapParams& mp, double* accq,
                        double* accw, int64_t PD, DevStatus* st, int num_sms, cudaStream_t s);
+void launch_footprints(const DevParticles& pt, const DevMapParams& mp, long long* rng, signed char* state,
+                       DevStatus* st, int num_sms, cudaStream_t s);
 void launch_reduce_2d(const double* acc, int64_t P, int nq, int reduce, double* out, cudaStream_t s);
 void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtype, int64_t n, const void* pos,
                     const void* hsml, const void* m, const void* rho, const void* q, const void* w,

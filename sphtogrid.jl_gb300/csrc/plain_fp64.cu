@@ -181,6 +181,36 @@ __global__ void __launch_bounds__(256) k_accumulate_finite(const double* __restr
   }
 }
 
+// Per-particle state and integer pixel ranges (sphg_footprints): the same
+// centring, filter, quantity skip and pix_index_min_max as every mapping
+// kernel (prep_particle_fp64).
+template <int DIMS>
+__global__ void __launch_bounds__(256) k_footprints(DevParticles pt, DevMapParams mp, long long* rng,
+                                                    signed char* state, DevStatus* st) {
+  unsigned flags = 0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pt.n; p += (int64_t)gridDim.x * blockDim.x) {
+    PrepFP64 q;
+    const int s = prep_particle_fp64<DIMS, false>(pt, mp, p, false, &q);
+    signed char code = 0;
+    long long r[6] = {0, 0, 0, 0, 0, 0};
+    if (s == kPrepMapped) {
+      code = 2;
+      for (int d = 0; d < DIMS; ++d) {
+        r[2 * d] = q.lo[d];
+        r[2 * d + 1] = q.hi[d];
+      }
+    } else if (s == kPrepZeroQ) {
+      code = 1;
+    } else if (s == kPrepNonFinite) {
+      code = 3;
+      flags |= kFlagNonFinite;
+    }
+    state[p] = code;
+    for (int k = 0; k < 6; ++k) rng[6 * p + k] = r[k];
+  }
+  if (flags) atomicOr(&st->flags, flags);
+}
+
 template <int DIMS>
 void launch_plain_dims(int kernel, const DevParticles& pt, const DevMapParams& mp, double* accq,
                        double* accw, int64_t PD, DevStatus* st, int grid, cudaStream_t s) {
@@ -229,6 +259,15 @@ void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
   k_reduce_3d<<<(int)grid, 256, 0, s>>>(q, w, PD, w_is_one, out);
+}
+
+void launch_footprints(const DevParticles& pt, const DevMapParams& mp, long long* rng, signed char* state,
+                       DevStatus* st, int num_sms, cudaStream_t s) {
+  int grid = (int)((pt.n + 255) / 256);
+  if (grid > num_sms * 8) grid = num_sms * 8;
+  if (grid < 1) grid = 1;
+  if (mp.dims == 2) k_footprints<2><<<grid, 256, 0, s>>>(pt, mp, rng, state, st);
+  else k_footprints<3><<<grid, 256, 0, s>>>(pt, mp, rng, state, st);
 }
 
 }  // namespace sphg

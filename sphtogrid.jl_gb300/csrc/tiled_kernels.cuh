@@ -269,23 +269,44 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
     }
     __syncwarp();
     const int F = ncol * dm.z;
+    // cell f = ab nz + c, from lane's first cell advanced by 32 per step
+    // (adds and selects instead of a division per cell)
     const float inv_nz = inv_small(dm.z);
+    int ab = fdiv(lane, inv_nz), c = lane - ab * dm.z;
+    const int dab = fdiv(32, inv_nz), dc = 32 - dab * dm.z;
     for (int f = lane; f < F; f += 32) {
-      const int ab = fdiv(f, inv_nz), c = f - ab * dm.z;
       cell_term_plane<DIMS, KERN>(kern, plane[ab], tab[2][c], hinv, s, comp, umin);
+      c += dc;
+      const bool w = c >= dm.z;
+      c = w ? c - dm.z : c;
+      ab += dab + (w ? 1 : 0);
     }
     __syncwarp();  // the tables are refilled for the next record
     return;
   }
   const int njk = dm.y * dm.z;
   const int F = dm.x * njk;
+  // cell f = (a nj + b) nk + c, advanced by 32 per step in that mixed radix
   const float inv_njk = inv_small(njk), inv_nz = inv_small(dm.z);
+  int a = fdiv(lane, inv_njk), b = lane - a * njk;
+  int c = DIMS == 3 ? b - fdiv(b, inv_nz) * dm.z : 0;
+  b = DIMS == 3 ? fdiv(b, inv_nz) : b;
+  const int da = fdiv(32, inv_njk), r32 = 32 - da * njk;
+  const int db = DIMS == 3 ? fdiv(r32, inv_nz) : r32, dc = DIMS == 3 ? r32 - db * dm.z : 0;
   for (int f = lane; f < F; f += 32) {
-    const int a = fdiv(f, inv_njk);
-    const int rr = f - a * njk;
-    const int b = DIMS == 3 ? fdiv(rr, inv_nz) : rr, c = DIMS == 3 ? rr - b * dm.z : 0;
     const float2 ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
     cell_term<DIMS, KERN>(kern, tab[0][a], tab[1][b], ez, hinv, s, comp, umin);
+    if (DIMS == 3) {
+      c += dc;
+      const bool wc = c >= dm.z;
+      c = wc ? c - dm.z : c;
+      b += db + (wc ? 1 : 0);
+    } else {
+      b += db;
+    }
+    const bool wb = b >= dm.y;
+    b = wb ? b - dm.y : b;
+    a += da + (wb ? 1 : 0);
   }
   __syncwarp();  // the tables are refilled for the next record
 }
@@ -817,19 +838,34 @@ __device__ __forceinline__ long long float_to_ll_split(float v) {
   return (long long)h * 2147483648LL + (long long)__float2int_rz(fmaf(-(float)h, 0x1p31f, v));
 }
 
-// Adds one cell value to a tile accumulator (see k_deposit).
+// Adds one cell value to a tile accumulator (see k_deposit).  DET: an exact
+// int64 fixed-point sum held as two 32-bit words, the low words in the first
+// plane (`hi`), the high words in the second (`lo`).  Shared-memory atomics on
+// 32-bit integers are single native instructions, while 64-bit and FP32 ones
+// are compiled to load / compare-and-swap loops; the low word's add returns
+// its old value, from which the carry into the high word follows, so the
+// pair adds exactly modulo 2^64 whatever the order of the additions.
 template <bool DET, bool SPLIT = false>
 __device__ __forceinline__ void acc_cell(float* hi, float* lo, unsigned long long* fx, int i, float v) {
   if (DET) {
-    atomicAdd(&fx[i], (unsigned long long)(SPLIT ? float_to_ll_split(v) : __float2ll_rn(v)));
+    const unsigned long long x = (unsigned long long)(SPLIT ? float_to_ll_split(v) : __float2ll_rn(v));
+    const unsigned xl = (unsigned)x;
+    const unsigned old = atomicAdd((unsigned*)hi + i, xl);
+    const unsigned xh = (unsigned)(x >> 32) + (old + xl < old ? 1u : 0u);
+    if (xh != 0u) atomicAdd((unsigned*)lo + i, xh);
   } else {
     acc_twosum(&hi[i], &lo[i], v);
   }
 }
 
+// The exact int64 value of a DET accumulator cell.
+__device__ __forceinline__ long long fixed_value(const float* hi, const float* lo, int i) {
+  return (long long)(((unsigned long long)((const unsigned*)lo)[i] << 32) | ((const unsigned*)hi)[i]);
+}
+
 template <bool DET>
 __device__ __forceinline__ double cell_value(const float* hi, const float* lo, const unsigned long long* fx, int i) {
-  if (DET) return (double)(long long)fx[i];
+  if (DET) return (double)fixed_value(hi, lo, i);
   return (double)hi[i] + (double)lo[i];
 }
 
@@ -1007,21 +1043,14 @@ __device__ __forceinline__ float channel_factor(float q, float cpm, int cpe, int
   return (cpm * qm) * pow2f(cpe + qe + shift);
 }
 
-// The cells of one (record, tile) pair: the intersection's n = na nb nc
-// cells, lane-strided, from the per-axis tables.  KERN is a compile-time
-// shape here.
+// One cell (a, b, c) of a pair's box.
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
-__device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
-                                              float cw, const float* cq, int nq, int TV, float* hi, float* lo,
-                                              unsigned long long* fx, int lane) {
-  const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
-  for (int e = lane; e < n; e += 32) {
-    const int bc = DIMS == 3 ? fdiv(e, inv_nc) : e;  // 2D: nc == 1
-    const int c = DIMS == 3 ? e - bc * nc : 0;
-    const int a = fdiv(bc, inv_nb);
-    const int b = bc - a * nb;
-    // 2D: the z term is the constant {0, 1} (the same u and weight as the
-    // renormalisation pass forms)
+__device__ __forceinline__ void deposit_cell(const float2 (*tab)[32], int a, int b, int c, int lbase, float hinv,
+                                             float cw, const float* cq, int nq, int TV, float* hi, float* lo,
+                                             unsigned long long* fx) {
+  // 2D: the z term is the constant {0, 1} (the same u and weight as the
+  // renormalisation pass forms)
+  {
     const float2 ex = tab[0][a], ey = tab[1][b], ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
     const float u = u_of((ex.x + ey.x) + ez.x, hinv);
     if (u <= 1.0f) {
@@ -1034,6 +1063,40 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
         acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li, gw * cq[k]);
       }
     }
+  }
+}
+
+// The cells of one (record, tile) pair: the intersection's n = na nb nc
+// cells, lane-strided, from the per-axis tables.  KERN is a compile-time
+// shape here.
+template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
+__device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
+                                              float cw, const float* cq, int nq, int TV, float* hi, float* lo,
+                                              unsigned long long* fx, int lane) {
+  // lane's first cell e = lane as (a, b, c); each step of 32 cells then
+  // advances it by 32 in the mixed radix (nb nc, nc) with adds and selects,
+  // so no cell pays a division (nor a conversion on the quarter-rate pipe)
+  const int nbc = nb * nc;
+  const float inv_nbc = inv_small(nbc), inv_nc = inv_small(nc);
+  int a = fdiv(lane, inv_nbc), b = lane - a * nbc;
+  int c = DIMS == 3 ? b - fdiv(b, inv_nc) * nc : 0;
+  b = DIMS == 3 ? fdiv(b, inv_nc) : b;
+  const int da = fdiv(32, inv_nbc), r32 = 32 - da * nbc;
+  const int db = DIMS == 3 ? fdiv(r32, inv_nc) : r32, dc = DIMS == 3 ? r32 - db * nc : 0;
+  for (int e = lane; e < n; e += 32) {
+    const int ca = a, cb = b, cc = c;
+    if (DIMS == 3) {
+      c += dc;
+      const bool wc = c >= nc;
+      c = wc ? c - nc : c;
+      b += db + (wc ? 1 : 0);
+    } else {
+      b += db;
+    }
+    const bool wb = b >= nb;
+    b = wb ? b - nb : b;
+    a += da + (wb ? 1 : 0);
+    deposit_cell<DIMS, KERN, NQ, TY, TZ, DET>(tab, ca, cb, cc, lbase, hinv, cw, cq, nq, TV, hi, lo, fx);
   }
 }
 
@@ -1234,7 +1297,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
       for (int c = 0; c <= nq; ++c) {
         if (DET) {
-          const unsigned long long x = fx[c * TV + li];
+          const unsigned long long x = (unsigned long long)fixed_value(hi, lo, c * TV + li);
           if (x) atomicAdd((unsigned long long*)A.acc + row + c * PD, x);
         } else {
           const double x = cell_value<DET>(hi, lo, fx, c * TV + li);

@@ -281,6 +281,61 @@ def _map_torch(Pos, HSML, M, Rho, Bin_Quant, Weights, param, kernel, reduce_imag
     return _shape_out(flat, P, nq, dims, return_both_maps and dims == 2), _stats_dict(st)
 
 
+def sph_footprints(Pos, HSML, Bin_Quant, *, param: MappingParameters, dimensions=2, calc_mean=False,
+                   context=None):
+    """Per-particle state and integer pixel ranges as the mapping computes
+    them on the device (sphg_footprints): centring and filter
+    (filter_shift.jl:6-58), the quantity skip (cic_2D.jl:154-168) and
+    pix_index_min_max (cic_shared.jl:46-52).  CUDA tensors in, on one device;
+    the positions are not written.  Returns ``(ranges, state)``: int64
+    (N, 6) ``[iMin, iMax, jMin, jMax, kMin, kMax]`` and int8 (N,) with 0
+    filtered, 1 skipped, 2 mapped."""
+    import torch
+    dims = dimensions
+    if dims not in (2, 3):
+        raise ValueError("dimensions must be 2 or 3")
+    if Pos.dim() != 2 or Pos.shape[0] != 3:
+        raise ValueError("Pos must be a (3, N) tensor")
+    dev = Pos.device
+    for a in (HSML, Bin_Quant):
+        if not _is_torch_cuda(a) or a.device != dev:
+            raise ValueError("all particle arrays must be CUDA tensors on the device of Pos")
+    adt = torch.float32 if HSML.dtype == torch.float32 and Bin_Quant.dtype == torch.float32 else torch.float64
+    hsml = HSML.to(adt).contiguous().reshape(-1)
+    q = Bin_Quant.to(adt)
+    nq = 1 if q.dim() == 1 else q.shape[0]
+    n = Pos.shape[1]
+    opts = _lib.SphgOptions()
+    opts.dimensions = dims
+    opts.kernel = 0
+    opts.kernel_dim = dims
+    opts.calc_mean = int(calc_mean)
+    opts.center = _lib.CENTER_READONLY
+    opts.filter = 1
+    opts.memspace = _lib.MEM_DEVICE
+    pt = _lib.SphgParticles()
+    pt.n = n
+    pt.pos_dtype = _torch_dt(Pos)
+    pt.attr_dtype = _torch_dt(hsml)
+    pt.pos = Pos.data_ptr()
+    pt.pos_stride_p, pt.pos_stride_c = Pos.stride(1), Pos.stride(0)
+    pt.hsml = hsml.data_ptr()
+    pt.bin_q = q.data_ptr()
+    pt.n_q = nq
+    if q.dim() == 1:
+        pt.q_stride_p, pt.q_stride_k = q.stride(0), 0
+    else:
+        pt.q_stride_p, pt.q_stride_k = q.stride(1), q.stride(0)
+    ranges = torch.empty((n, 6), dtype=torch.int64, device=dev)
+    state = torch.empty(n, dtype=torch.int8, device=dev)
+    ctx = context if context is not None else _lib.default_context(dev.index if dev.index is not None else 0)
+    stream = _lib.stream_handle(torch.cuda.current_stream(dev))
+    _lib.check(_lib.lib().sphg_footprints(ctx.handle, C.byref(param._c), C.byref(opts), C.byref(pt),
+                                          C.c_void_p(ranges.data_ptr()), C.c_void_p(state.data_ptr()), stream),
+               ctx.handle)
+    return ranges, state
+
+
 def rotation_matrix_xyz(alpha: float, beta: float, gamma: float) -> np.ndarray:
     """RotXYZ(alpha, beta, gamma) = Rx(alpha) Ry(beta) Rz(gamma), angles in
     degrees, as rotate_3D builds it (rotate_particles.jl:7-14); row-major."""
