@@ -47,7 +47,7 @@ typedef enum sphg_status {
   SPHG_ERR_DIMS = 3,          /* dimensions not 2 or 3 (the reference returns `nothing`) */
   SPHG_ERR_NONFINITE = 4,     /* non-finite pixel range of a mapped particle (the
                                  reference's floor(Integer, x) throws InexactError,
-                                 cic_shared.jl:292-293) */
+                                 cic_shared.jl:46-52) */
   SPHG_ERR_NQ = 5,            /* 3D maps a single scalar quantity (cic_3D.jl:140) */
   SPHG_ERR_ALLOC = 6,         /* device or host allocation failed */
   SPHG_ERR_ARG = 7,           /* null pointer, bad dtype, bad stride, bad size */
@@ -144,7 +144,7 @@ typedef struct sphg_stats {
   int64_t deposits;      /* sum of integer footprints of mapped particles */
   double grid_mass;      /* 3D mass diagnostic (cic_3D.jl:186) */
   double particle_mass;  /* 3D: sum of mapped particle masses (cic_3D.jl:192) */
-  sphg_params centred;   /* parameters re-derived around centre 0 (filter_shift.jl:292) */
+  sphg_params centred;   /* parameters re-derived around centre 0 (filter_shift.jl:25-31) */
   int32_t n_launches;    /* kernels this call launched */
   int32_t n_reruns;      /* FP32C: re-runs after growing the tile-pair list */
   float phase_ms[4];     /* with profile: device milliseconds per SPHG_PHASE_* */
@@ -293,22 +293,32 @@ int sphg_footprints(sphg_context *ctx, const sphg_params *par, const sphg_option
  *
  * sphg_map_noalloc maps like sphg_map with precision FP32C, but needs no
  * context and calls no cudaMalloc, cudaFree or allocating library routine.
- * Its scratch (particle records, tile lists, the (particle, tile) overlap
- * list, the status word) is one static device array of
+ * Its scratch (particle records, tile lists, the (particle, tile) pair
+ * records, the status word) is one static device array of
  * SPHG_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
- * the process exits.  Limits: records take (72 + 4 n_q) bytes per input
- * particle and the overlap list 4 bytes per (particle, tile) pair, so a few
- * hundred thousand particles fit; larger calls return SPHG_ERR_ARG (before
- * any work) or SPHG_ERR_ALLOC (overlap list full) -- use sphg_map for them.
+ * the process exits.  Limits: records take (84 + 4 n_q) bytes per input
+ * particle; of what remains, about an eighth holds large-footprint chunk
+ * sums and the rest the pair records, 64 bytes per (particle, tile) overlap,
+ * so a few hundred thousand particles fit.  Larger calls return
+ * SPHG_ERR_ARG (before any work) or SPHG_ERR_ALLOC (pair records full) --
+ * use sphg_map for them.
  *
  * - Device memory only (opt->memspace = SPHG_MEM_DEVICE); runs on the
- *   caller's current device and `stream` (NULL: the legacy default stream)
- *   and returns when the map is complete.
+ *   caller's current device and `stream` (NULL: the legacy default stream),
+ *   synchronises that stream and returns when the map is complete.
+ * - SPHG_CENTER_INPLACE: the map centres on the fly and the centred
+ *   positions are written back only when the map completes (or meets a
+ *   non-finite value, as the reference does); a call that returns
+ *   SPHG_ERR_ALLOC leaves the positions as they were, so a retry with the
+ *   same options (through sphg_map) centres them once.
  * - The first call on a device looks up the array's device address
- *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   (cudaGetSymbolAddress) and keeps it for the process; make that first
+ *   call before any stream capture.  The kept address is not valid after a
+ *   cudaDeviceReset of that device.
  * - Every call on a device shares the one array and clears what it
  *   accumulates into; calls that overlap on the GPU (other streams or host
  *   threads without ordering between them) race and corrupt each other.
+ * - opt->profile is ignored (no phase timings); opt->reserved must be 0.
  * - Errors: sphg_last_error(NULL) gives the message (per host thread). */
 #define SPHG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 

@@ -39,7 +39,7 @@ enum {
   ORC_ERR_CENTER_EXTENT = 1, /* parameters.jl:67 */
   ORC_ERR_PIXELS = 2,        /* parameters.jl:98 */
   ORC_ERR_DIMS = 3,          /* sphMapping returns `nothing`: cic_interpolation.jl:148,217 */
-  ORC_ERR_NONFINITE = 4,     /* floor(Integer, NaN) throws: cic_shared.jl:292-293 */
+  ORC_ERR_NONFINITE = 4,     /* floor(Integer, NaN) throws: cic_shared.jl:46-52 */
   ORC_ERR_NQ = 5,            /* 3D maps one scalar quantity: cic_3D.jl:140 */
   ORC_ERR_ALLOC = 6,
   ORC_ERR_ARG = 7
@@ -142,7 +142,7 @@ static inline void st(int dtype, void *p, int64_t i, double v) {
 
 /* center_particles, filter_shift.jl:6-32.  Shifts the caller's positions IN
  * PLACE (in their own precision) and returns the parameters re-derived around
- * centre 0, as the reference does via the constructor (:292-294). */
+ * centre 0, as the reference does via the constructor (filter_shift.jl:25-31). */
 int orc_center_particles(int pos_dtype, void *pos, int64_t n, int64_t sp,
                          int64_t sc, const orc_params *par, orc_params *out) {
   const double cen[3] = {par->center[0], par->center[1], par->center[2]};

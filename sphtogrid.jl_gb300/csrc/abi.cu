@@ -313,7 +313,7 @@ int map_impl(sphg_context* ctx, const sphg_params* par, const sphg_options* opt,
   const int64_t PD = dims == 2 ? P * P : P * P * P;
   const int64_t out_len = sphg_output_len(par, opt, nq);
 
-  // centred parameters, re-derived as center_particles does (filter_shift.jl:288-294)
+  // centred parameters, re-derived as center_particles does (filter_shift.jl:25-31)
   sphg_params cpar;
   {
     const double* cen = par->center;
