@@ -220,7 +220,7 @@ def bench_gpu(args):
         import __graft_entry__ as graft
         tun = tuple(int(x) for x in args.batched_tuning.split(",")) if args.batched_tuning else None
         b = bench_batched(graft.load_package(), dev, args.steps, args.warmup, args.batched_maps,
-                          args.deterministic, tun)
+                          args.deterministic, tun, with_oracle=False)
         if rank == 0:
             b.pop("rel_err_per_map")
             print(json.dumps(b), flush=True)
@@ -324,9 +324,12 @@ def bench_gpu(args):
                  "phases_ms": {"prep": float(ph2[0]), "norm": float(ph2[1]),
                                "deposit": float(ph2[2]), "reduce": float(ph2[3])},
                  "rel_linf_vs_fp64": _rel_linf(t_out.cpu().numpy(), img_fp64.cpu().numpy())}
-    batched = None
+    batched = config1 = diff = None
     if rank == 0 and world == 1 and not args.no_batched:
-        batched = bench_batched(pkg, dev, args.steps, args.warmup)
+        batched = bench_batched(pkg, dev, args.steps, args.warmup, with_oracle=not args.no_cpu_baseline)
+    if rank == 0 and world == 1 and not args.no_sub_workloads:
+        config1 = bench_config1(pkg, dev, args.steps, args.warmup)
+        diff = bench_differentiable(pkg, dev, min(args.steps, 3), 1)
 
     # end to end through the C ABI with pinned host buffers
     h_pos = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).pin_memory()
@@ -389,6 +392,10 @@ def bench_gpu(args):
         line["onchip_ceiling"] = _onchip_ceiling(L, ctx, _lib, value, other, args.deterministic)
     if batched is not None:
         line["batched"] = batched
+    if config1 is not None:
+        line["projection_2d"] = config1
+    if diff is not None:
+        line["differentiable"] = diff
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         O = oracle_module()
         dt, dep, img_ref, threads, m = run_oracle(O, d, frac=args.cpu_frac)
@@ -406,6 +413,86 @@ def bench_gpu(args):
     return 0
 
 
+CONFIG1_WORKLOAD = ("2D projected map: N=2^18 Float64 particles uniform in the unit cube, hsml lognormal "
+                    "(median 0.01, sigma 0.5) clipped to [0.002, 0.1], m = 1/N, rho uniform in [0.5, 2], "
+                    "Bin_Quant = Weights = rho, Cubic, 256^2, reduce_image=true, seed 0")
+
+
+def _weighted_errors(got, ref, W, absq_ref=None):
+    """Relative L-infinity of `got` against `ref` on the pixels carrying
+    weight (W >= 1e-6 max W): plainly relative to each pixel's value, and
+    relative to the map of |q| (the same map where every q > 0)."""
+    got = np.asarray(got, dtype=np.float64).reshape(-1)
+    ref = np.asarray(ref, dtype=np.float64).reshape(-1)
+    W = np.asarray(W, dtype=np.float64).reshape(-1)
+    keep = W >= 1e-6 * W.max()
+    d = np.abs(got - ref)
+    a = np.abs(ref)
+    plain = float((d[keep & (a > 0)] / a[keep & (a > 0)]).max()) if (keep & (a > 0)).any() else 0.0
+    if absq_ref is None:
+        return plain, plain
+    sc = np.maximum(a, np.abs(np.asarray(absq_ref, dtype=np.float64).reshape(-1)))
+    sel = keep & (sc > 0)
+    return plain, (float((d[sel] / sc[sel]).max()) if sel.any() else 0.0)
+
+
+def bench_config1(pkg, dev, steps, warmup):
+    """The 2D projected map (the reference's CPU-runnable case) at full size:
+    FP32C and plain FP64 maps/s on the GPU, each against the oracle on the
+    pixels carrying weight, and the oracle on all host threads."""
+    import torch
+    from sphtogrid_gb300 import synth
+    d = synth.uniform_2d()
+    P = d["npix"]
+    par = pkg.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+    tp = torch.from_numpy(np.ascontiguousarray(d["pos"].T)).to(dev).T
+    ts = [torch.from_numpy(np.ascontiguousarray(d[k])).to(dev) for k in ("hsml", "mass", "rho", "bin_q", "weights")]
+    stream = torch.cuda.current_stream(dev)
+
+    def run(prec, k, w):
+        img = st = None
+        for _ in range(w):
+            img, st = pkg.sphMapping(tp, *ts, param=par, kernel=pkg.Cubic(2), precision=prec, show_progress=False,
+                                     return_stats=True, center_in_place=False)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            img, st = pkg.sphMapping(tp, *ts, param=par, kernel=pkg.Cubic(2), precision=prec, show_progress=False,
+                                     return_stats=True, center_in_place=False)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / k, img.cpu().numpy(), st
+
+    ms32, img32, st = run("fp32c", steps, warmup)
+    ms64, img64, _ = run("fp64", max(2, steps // 2), 1)
+    O = oracle_module()
+    opar = O.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+    threads = os.cpu_count() or 1
+    args = (d["hsml"], d["mass"], d["rho"], d["bin_q"], d["weights"])
+    t0 = time.perf_counter()
+    ref, info = O.sph_mapping(d["pos"].copy(order="F"), *args, param=opar, kernel="cubic", dimensions=2,
+                              nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    raw, _ = O.sph_mapping(d["pos"].copy(order="F"), *args, param=opar, kernel="cubic", dimensions=2,
+                           return_both_maps=True, nthreads=threads)
+    W = raw[:, -1].reshape(P, P)  # raw rows x*P + y -> [x, y]
+    ref = np.asarray(ref).reshape(P, P)
+    e32 = _weighted_errors(img32.reshape(P, P), ref, W)[0]
+    e64 = _weighted_errors(img64.reshape(P, P), ref, W)[0]
+    dep = st["deposits"]
+    assert dep == info["deposits"], (dep, info["deposits"])
+    return {"workload": CONFIG1_WORKLOAD, "particles": int(d["pos"].shape[1]), "deposits_per_map": int(dep),
+            "fp32c": {"ms_per_map": ms32, "maps_per_s": 1e3 / ms32, "deposits_per_s": dep / (ms32 * 1e-3),
+                      "rel_linf_vs_oracle": e32},
+            "plain_fp64": {"ms_per_map": ms64, "maps_per_s": 1e3 / ms64, "deposits_per_s": dep / (ms64 * 1e-3),
+                           "rel_linf_vs_oracle": e64},
+            "speedup_fp32c_vs_fp64": ms64 / ms32,
+            "error_norm": "relative L-infinity on pixels with W >= 1e-6 max W (q = rho > 0)",
+            "cpu_baseline": {"kind": "port", "cores": threads, "sample": "the whole map",
+                             "ms_per_map": cpu_s * 1e3, "deposits_per_s": dep / cpu_s}}
+
+
 BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e6], Npixels in "
                   "{128, 256, 512, 1024}, 1-4 quantities (rho, lognormal temperature, Gaussian "
                   "velocity component sigma 300, lognormal |B|), Quintic and WendlandC4 mixed, "
@@ -413,11 +500,12 @@ BATCH_WORKLOAD = ("96 independent 2D maps, particle counts lognormal in [1e4, 2e
                   "autotuned tiles")
 
 
-def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tuning=None):
+def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tuning=None, with_oracle=True):
     """The batched uneven-maps workload: maps/s of one graph-replayed batch
-    against the plain FP64 method called map by map, and each map's error
-    against the plain FP64 map (on pixels with W >= 1e-6 max W, relative to
-    the map of |q| where quantities of both signs cancel)."""
+    against the plain FP64 method called map by map, each map's error against
+    the plain FP64 map (on pixels with W >= 1e-6 max W, relative to the value
+    and relative to the map of |q| where quantities of both signs cancel),
+    and eight maps spanning the particle counts against the oracle."""
     import torch
     from sphtogrid_gb300 import synth
     from sphtogrid_gb300.batch import MapSpec, SPHBatch
@@ -463,21 +551,39 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tunin
     e1.record(stream)
     torch.cuda.synchronize(dev)
     ms64 = e0.elapsed_time(e1)
-    errs = []
+    errs, errs_plain = [], []
+    # maps also checked against the oracle: 8 spanning the particle counts
+    by_n = np.argsort([d["pos"].shape[1] for d in maps], kind="stable")
+    pick = sorted(set(int(by_n[k]) for k in np.linspace(0, len(maps) - 1, min(8, len(maps))).round().astype(int)))
+    vs_oracle = []
+    O = oracle_module() if with_oracle else None
     for i, x in enumerate(host):
         par = x[0]
         P = int(par.Npixels[0])
         raw = one(*x, raw=True).cpu().numpy()
         absq = one(*x, q=x[2][3].abs(), raw=True).cpu().numpy()
+        if O is not None and i in pick:
+            dm = maps[i]
+            opar = O.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=P)
+            oraw, _ = O.sph_mapping(dm["pos"].copy(order="F"), dm["hsml"], dm["mass"], dm["rho"], dm["bin_q"],
+                                    dm["weights"], param=opar, kernel=dm["kernel"], dimensions=2,
+                                    return_both_maps=True, nthreads=os.cpu_count() or 1)
+            oW = oraw[:, -1:]
+            onq = oraw.shape[1] - 1
+            oref = np.where(oW > 0, oraw[:, :onq] / np.where(oW > 0, oW, 1.0), oraw[:, :onq])
+            oabs = np.where(oW > 0, absq[:, :onq] / np.where(oW > 0, oW, 1.0), absq[:, :onq])
+            ogot = b.image(i).cpu().numpy().reshape(P * P, onq)
+            ep, es = _weighted_errors(ogot, oref, np.repeat(oW, onq, axis=1), oabs)
+            vs_oracle.append({"map": i, "particles": int(dm["pos"].shape[1]), "npix": P, "quantities": onq,
+                              "rel_linf_plain": ep, "rel_linf_absq_scaled": es})
         W = raw[:, -1:]
         nq = raw.shape[1] - 1
         ref = np.where(W > 0, raw[:, :nq] / np.where(W > 0, W, 1.0), raw[:, :nq])
         scale = np.where(W > 0, absq[:, :nq] / np.where(W > 0, W, 1.0), absq[:, :nq])
         got = b.image(i).cpu().numpy().reshape(P * P, nq)  # [x, y, q] -> rows x*P + y
-        keep = np.repeat(W >= 1e-6 * W.max(), nq, axis=1)
-        den = np.maximum(np.abs(ref), scale)
-        sel = keep & (den > 0)
-        errs.append(float((np.abs(got - ref)[sel] / den[sel]).max()) if sel.any() else 0.0)
+        ep, es = _weighted_errors(got, ref, np.repeat(W, nq, axis=1), scale)
+        errs.append(es)
+        errs_plain.append(ep)
     n = len(maps)
     out = {"workload": BATCH_WORKLOAD, "maps": n,
            "particles": int(sum(d["pos"].shape[1] for d in maps)),
@@ -486,6 +592,11 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tunin
            "plain_fp64_maps_per_s": 1e3 * n / ms64, "speedup_vs_plain_fp64": ms64 / ms_batch,
            "rel_err_max": max(errs), "rel_err_median": float(np.median(errs)),
            "rel_err_per_map": [float(f"{e:.3g}") for e in errs],
+           "rel_err_plain_max": max(errs_plain),
+           "error_norms": ("against the plain FP64 map of each map, on pixels with W >= 1e-6 max W: "
+                           "rel_err_* relative to the map of |q| (the value itself where q > 0), "
+                           "rel_err_plain_* relative to the value itself"),
+           "vs_oracle": vs_oracle,
            "deterministic": bool(deterministic), "tuning": b.tuning,
            "plan_and_autotune_s": plan_s}
     b.close()
@@ -746,6 +857,8 @@ def main():
                     help="time the device-resident loop only (for profiler runs)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched 96-map workload")
+    ap.add_argument("--no-sub-workloads", action="store_true",
+                    help="skip the 2D projection and differentiable sub-records")
     ap.add_argument("--batched-only", action="store_true",
                     help="time the batched workload alone (for profiler runs)")
     ap.add_argument("--batched-maps", type=int, default=96,

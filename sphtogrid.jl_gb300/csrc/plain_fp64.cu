@@ -25,6 +25,35 @@ __device__ __forceinline__ long long warp_sum(long long v) {
   return v;
 }
 
+// Footprint cell f = (ia nj + jb) nk + kc of a lane-strided walk: the lane's
+// first cell is decomposed once, then each step of 32 cells advances
+// (ia, jb, kc) in that mixed radix with adds and compares -- no 64-bit
+// integer division per cell (the same cells, in the same order).
+struct CellWalk {
+  int64_t ia, jb, kc;
+  int64_t da, db, dc, nj, nk;
+  __device__ __forceinline__ CellWalk(int lane, int64_t nj_, int64_t nk_) : nj(nj_), nk(nk_) {
+    const int64_t njk = nj * nk;
+    ia = lane / njk;
+    const int64_t r = lane - ia * njk;
+    jb = r / nk;
+    kc = r - jb * nk;
+    da = 32 / njk;
+    const int64_t r32 = 32 - da * njk;
+    db = r32 / nk;
+    dc = r32 - db * nk;
+  }
+  __device__ __forceinline__ void step() {
+    kc += dc;
+    const bool wk = kc >= nk;
+    kc = wk ? kc - nk : kc;
+    jb += db + (wk ? 1 : 0);
+    const bool wj = jb >= nj;
+    jb = wj ? jb - nj : jb;
+    ia += da + (wj ? 1 : 0);
+  }
+};
+
 // One warp deposits one particle: pass 1 sums kernel x area weights over the
 // footprint (calculate_weights), pass 2 recomputes them and adds the
 // renormalised weight to the image (update_image!).
@@ -55,9 +84,9 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
     // pass 1: calculate_weights (cic_2D.jl:11-72 / cic_3D.jl:13-78)
     double s_w = 0.0, s_a = 0.0;
     long long n_d = 0, n_t = 0;
-    for (int64_t f = lane; f < F; f += 32) {
-      const int64_t ia = f / njk, r = f - ia * njk;
-      const int64_t jb = r / nk, kc = r - jb * nk;
+    CellWalk w1(lane, nj, nk);
+    for (int64_t f = lane; f < F; f += 32, w1.step()) {
+      const int64_t ia = w1.ia, jb = w1.jb, kc = w1.kc;
       double u, a;
       cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &u, &a);
       s_a += a;
@@ -84,10 +113,9 @@ __global__ void __launch_bounds__(256) k_plain_fp64(DevParticles pt, DevMapParam
 
     // pass 2: deposit (cic_2D.jl:193-222, cic_3D.jl:172-188)
     double gm = 0.0;
-    for (int64_t f = lane; f < F; f += 32) {
-      const int64_t ia = f / njk, r = f - ia * njk;
-      const int64_t jb = r / nk, kc = r - jb * nk;
-      const int64_t i = iMin + ia, j = jMin + jb, k = kMin + kc;
+    CellWalk w2(lane, nj, nk);
+    for (int64_t f = lane; f < F; f += 32, w2.step()) {
+      const int64_t i = iMin + w2.ia, j = jMin + w2.jb, k = kMin + w2.kc;
       double u, a;
       cell_fp64<DIMS>(q, i, j, k, &u, &a);
       const double wk = fallback ? 1.0 : (u <= 1.0 ? kshape<KERN, double>(u) * q.knorm : 0.0);

@@ -269,44 +269,23 @@ __device__ __forceinline__ void record_sum_tab(int kern, const float4 g, const i
     }
     __syncwarp();
     const int F = ncol * dm.z;
-    // cell f = ab nz + c, from lane's first cell advanced by 32 per step
-    // (adds and selects instead of a division per cell)
     const float inv_nz = inv_small(dm.z);
-    int ab = fdiv(lane, inv_nz), c = lane - ab * dm.z;
-    const int dab = fdiv(32, inv_nz), dc = 32 - dab * dm.z;
     for (int f = lane; f < F; f += 32) {
+      const int ab = fdiv(f, inv_nz), c = f - ab * dm.z;
       cell_term_plane<DIMS, KERN>(kern, plane[ab], tab[2][c], hinv, s, comp, umin);
-      c += dc;
-      const bool w = c >= dm.z;
-      c = w ? c - dm.z : c;
-      ab += dab + (w ? 1 : 0);
     }
     __syncwarp();  // the tables are refilled for the next record
     return;
   }
   const int njk = dm.y * dm.z;
   const int F = dm.x * njk;
-  // cell f = (a nj + b) nk + c, advanced by 32 per step in that mixed radix
   const float inv_njk = inv_small(njk), inv_nz = inv_small(dm.z);
-  int a = fdiv(lane, inv_njk), b = lane - a * njk;
-  int c = DIMS == 3 ? b - fdiv(b, inv_nz) * dm.z : 0;
-  b = DIMS == 3 ? fdiv(b, inv_nz) : b;
-  const int da = fdiv(32, inv_njk), r32 = 32 - da * njk;
-  const int db = DIMS == 3 ? fdiv(r32, inv_nz) : r32, dc = DIMS == 3 ? r32 - db * dm.z : 0;
   for (int f = lane; f < F; f += 32) {
+    const int a = fdiv(f, inv_njk);
+    const int rr = f - a * njk;
+    const int b = DIMS == 3 ? fdiv(rr, inv_nz) : rr, c = DIMS == 3 ? rr - b * dm.z : 0;
     const float2 ez = DIMS == 3 ? tab[2][c] : make_float2(0.0f, 1.0f);
     cell_term<DIMS, KERN>(kern, tab[0][a], tab[1][b], ez, hinv, s, comp, umin);
-    if (DIMS == 3) {
-      c += dc;
-      const bool wc = c >= dm.z;
-      c = wc ? c - dm.z : c;
-      b += db + (wc ? 1 : 0);
-    } else {
-      b += db;
-    }
-    const bool wb = b >= dm.y;
-    b = wb ? b - dm.y : b;
-    a += da + (wb ? 1 : 0);
   }
   __syncwarp();  // the tables are refilled for the next record
 }

@@ -114,6 +114,38 @@ function context()
     return CTX[]
 end
 
+# Particles already centred and selected (sort_z): mapped with no further
+# centring or filtering (SPHG_CENTER_NONE, filter 0).
+function map_selected(pos, HSML, M, Rho, Bin_Quant, Weights, par_c, kernel, show_progress, reduce_image,
+                      return_both_maps, dimensions, calc_mean, precision)
+    T = (eltype(HSML) == Float32 && eltype(M) == Float32 && eltype(Rho) == Float32 &&
+         eltype(Bin_Quant) == Float32 && eltype(Weights) == Float32) ? Float32 : Float64
+    pos = eltype(pos) <: Union{Float32,Float64} ? pos : Float64.(pos)
+    hsml, m, rho, w, q = T.(HSML), T.(M), T.(Rho), T.(Weights), T.(Bin_Quant)
+    N = length(m)
+    nq = ndims(q) == 1 ? 1 : size(q, 1)
+    P = par_c.Npixels[1]
+    out = return_both_maps && dimensions == 2 ? zeros(Float64, P * P, nq + 1) :
+          dimensions == 2 ? zeros(Float64, P, P, nq) : zeros(Float64, P, P, P)
+    st = SphgStats()
+    GC.@preserve pos hsml m rho w q out begin
+        pt = SphgParticles(N, dtype_id(eltype(pos)), dtype_id(T), pointer(pos), 3, 1,
+                           pointer(hsml), pointer(m), pointer(rho), pointer(w), pointer(q),
+                           Int32(nq), Int32(0), ndims(q) == 1 ? 1 : nq, ndims(q) == 1 ? 0 : 1)
+        kdim = hasfield(typeof(kernel), :dim) ? Int32(kernel.dim) : Int32(3)
+        opt = SphgOptions(dimensions, kernel_id(kernel), kdim, reduce_image, return_both_maps,
+                          calc_mean, precision === :fp32c ? 1 : 0, 0, 0, 0, 1, 0, 0, (0, 0, 0))
+        status = ccall((:sphg_map, libsphgrid), Cint,
+                       (Ptr{Cvoid}, Ref{SphgParams}, Ref{SphgOptions}, Ref{SphgParticles},
+                        Ptr{Float64}, Ptr{Cvoid}, Ref{SphgStats}),
+                       context(), SphgParams(par_c), opt, pt, pointer(out), C_NULL, st)
+        status == 0 || error(unsafe_string(ccall((:sphg_last_error, libsphgrid), Cstring,
+                                                 (Ptr{Cvoid},), context())))
+    end
+    show_progress && @info "Particles in image: $(st.n_mapped) / $N, deposits: $(st.deposits)"
+    return out
+end
+
 """
     sphMapping(Pos, HSML, M, Rho, Bin_Quant, Weights=Rho, RM=nothing;
                param, kernel, show_progress=true, parallel=false, reduce_image=true,
@@ -121,7 +153,12 @@ end
                sort_z=false, precision=:fp64)
 
 The reference's `sphMapping` on the GPU.  `parallel` is ignored (one GPU);
-`RM`/`stokes` (Faraday rotation) and `sort_z` are not supported here.
+`RM`/`stokes` (Faraday rotation) are not supported here.  With `sort_z` the
+selection is the reference's own host glue (`center_particles` on the
+caller's array, then `filter_particles_in_image(..., true)`: the z-sorted
+index list taken at the input-order in-image mask, filter_shift.jl:6-64),
+and the gathered particles are mapped on the GPU without further centring
+or filtering.
 """
 function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
                     Rho::Array{<:Real}, Bin_Quant::Array{<:Real},
@@ -132,8 +169,14 @@ function sphMapping(Pos::Array{<:Real}, HSML::Array{<:Real}, M::Array{<:Real},
                     dimensions::Int=2, calc_mean::Bool=false, stokes::Bool=false,
                     sort_z::Bool=false, precision::Symbol=:fp64)
     (RM === nothing && !stokes) || error("Faraday rotation is not supported by the GPU path")
-    sort_z && error("sort_z is not supported by the GPU path")
     dimensions in (2, 3) || return nothing
+    if sort_z
+        Pos, par_c = SPHtoGrid.center_particles(Pos, param)  # in place, as the reference
+        sel = SPHtoGrid.filter_particles_in_image(Pos, par_c, true)
+        q_sel = ndims(Bin_Quant) == 1 ? Bin_Quant[sel] : Bin_Quant[:, sel]
+        return map_selected(Pos[:, sel], HSML[sel], M[sel], Rho[sel], q_sel, Weights[sel], par_c, kernel,
+                            show_progress, reduce_image, return_both_maps, dimensions, calc_mean, precision)
+    end
     T = (eltype(HSML) == Float32 && eltype(M) == Float32 && eltype(Rho) == Float32 &&
          eltype(Bin_Quant) == Float32 && eltype(Weights) == Float32) ? Float32 : Float64
     pos = eltype(Pos) <: Union{Float32,Float64} ? Pos : Float64.(Pos)
@@ -291,7 +334,16 @@ is the forward's, `adjoint_precision` (default: the same) the pullback's:
 `:fp64`, or `:fp32c` (per-cell terms in FP32 with compensated sums, particles
 whose sums cancel beyond the FP32 rounding estimate redone in FP64).
 """
-function sphMapping_differentiable end
+function sphMapping_differentiable(Pos, HSML, M, Rho, Bin_Quant, Weights; param::mappingParameters,
+                                   kernel::AbstractSPHKernel, dimensions::Int=2, reduce_image::Bool=true,
+                                   precision::Symbol=:fp64, adjoint_precision::Symbol=precision)
+    # outside automatic differentiation: the forward of the rule, pullback dropped
+    out, _ = ChainRulesCore.rrule(sphMapping_differentiable, Pos, HSML, M, Rho, Bin_Quant, Weights;
+                                  param=param, kernel=kernel, dimensions=dimensions,
+                                  reduce_image=reduce_image, precision=precision,
+                                  adjoint_precision=adjoint_precision)
+    return out
+end
 
 function ChainRulesCore.rrule(::typeof(sphMapping_differentiable), Pos, HSML, M, Rho, Bin_Quant,
                               Weights; param::mappingParameters, kernel::AbstractSPHKernel,
