@@ -574,8 +574,14 @@ def bench_batched(pkg, dev, steps, warmup, n_maps=96, deterministic=False, tunin
             oabs = np.where(oW > 0, absq[:, :onq] / np.where(oW > 0, oW, 1.0), absq[:, :onq])
             ogot = b.image(i).cpu().numpy().reshape(P * P, onq)
             ep, es = _weighted_errors(ogot, oref, np.repeat(oW, onq, axis=1), oabs)
+            # channels whose quantity has one sign: there Q / W cannot cancel
+            qk = np.asarray(dm["bin_q"], dtype=np.float64).reshape(onq, -1)
+            one_sign = [k for k in range(onq) if qk[k].min() >= 0.0 or qk[k].max() <= 0.0]
+            e1 = _weighted_errors(ogot[:, one_sign], oref[:, one_sign], np.repeat(oW, len(one_sign), axis=1))[0] \
+                if one_sign else None
             vs_oracle.append({"map": i, "particles": int(dm["pos"].shape[1]), "npix": P, "quantities": onq,
-                              "rel_linf_plain": ep, "rel_linf_absq_scaled": es})
+                              "rel_linf_absq_scaled": es, "rel_linf_plain": ep,
+                              "rel_linf_plain_single_sign_channels": e1})
         W = raw[:, -1:]
         nq = raw.shape[1] - 1
         ref = np.where(W > 0, raw[:, :nq] / np.where(W > 0, W, 1.0), raw[:, :nq])

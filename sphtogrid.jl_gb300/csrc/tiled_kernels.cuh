@@ -906,6 +906,7 @@ struct DepositShared {
   int shift[kMaxQ + 1];
   double bnd[kMaxQ + 1][8];  // deterministic mode: per-warp tile bounds
   float2 tabs[8][3][32];     // per-warp axis tables of the current pair
+  uint4 small[8][16][4];     // per-warp constants of the packed small pairs (deposit_small)
   uint4 stage[8][2][kStage * kPairRecWords];  // per-warp double buffer of pair records
   unsigned long long bar[8][2];               // mbarriers of the staging buffers
   unsigned phase[8];         // per warp: bit b, the parity buffer b's barrier waits for next
@@ -1052,29 +1053,12 @@ template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
 __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
                                               float cw, const float* cq, int nq, int TV, float* hi, float* lo,
                                               unsigned long long* fx, int lane) {
-  // lane's first cell e = lane as (a, b, c); each step of 32 cells then
-  // advances it by 32 in the mixed radix (nb nc, nc) with adds and selects,
-  // so no cell pays a division (nor a conversion on the quarter-rate pipe)
-  const int nbc = nb * nc;
-  const float inv_nbc = inv_small(nbc), inv_nc = inv_small(nc);
-  int a = fdiv(lane, inv_nbc), b = lane - a * nbc;
-  int c = DIMS == 3 ? b - fdiv(b, inv_nc) * nc : 0;
-  b = DIMS == 3 ? fdiv(b, inv_nc) : b;
-  const int da = fdiv(32, inv_nbc), r32 = 32 - da * nbc;
-  const int db = DIMS == 3 ? fdiv(r32, inv_nc) : r32, dc = DIMS == 3 ? r32 - db * nc : 0;
+  const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
   for (int e = lane; e < n; e += 32) {
-    const int ca = a, cb = b, cc = c;
-    if (DIMS == 3) {
-      c += dc;
-      const bool wc = c >= nc;
-      c = wc ? c - nc : c;
-      b += db + (wc ? 1 : 0);
-    } else {
-      b += db;
-    }
-    const bool wb = b >= nb;
-    b = wb ? b - nb : b;
-    a += da + (wb ? 1 : 0);
+    const int bc = DIMS == 3 ? fdiv(e, inv_nc) : e;  // 2D: nc == 1
+    const int cc = DIMS == 3 ? e - bc * nc : 0;
+    const int ca = fdiv(bc, inv_nb);
+    const int cb = bc - ca * nb;
     deposit_cell<DIMS, KERN, NQ, TY, TZ, DET>(tab, ca, cb, cc, lbase, hinv, cw, cq, nq, TV, hi, lo, fx);
   }
 }
@@ -1129,6 +1113,89 @@ __device__ __forceinline__ void deposit_pair32(const TiledArgs& A, const uint4* 
   else SPHG_CELLS(4);
 #undef SPHG_CELLS
   __syncwarp();  // the tables are refilled for the next pair
+}
+
+// Pairs of at most this many cells are deposited packed: the small pairs of
+// a staged chunk share the warp's iterations, lanes taking consecutive cells
+// across them, instead of one pair (and its axis tables) per iteration.
+constexpr int kSmallCells = 32;
+
+// The per-pair constants of a packed small pair, prepared by its lane
+// (four uint4): {fx, fy, fz, h}, {1/h, cw, a0, b0}, {c0, pack, inv_nc,
+// inv_nbc}, {cq[0..3]} -- the channel factors with this tile's shifts.
+template <int DIMS, int NQ>
+__device__ __forceinline__ void small_header(const uint4* R, const int* s_shift, int nq, uint4* H) {
+  const uint4 g = R[0], m = R[1], o = R[2], q4 = R[3];
+  const unsigned pack = m.w;
+  const int nb = (int)((pack >> 15) & 31u) + 1;
+  const int nc = DIMS == 3 ? (int)((pack >> 20) & 31u) + 1 : 1;
+  const float cpm = __uint_as_float(m.y);
+  const int cpe = (int)m.z;
+  const float cw = cpm * pow2f(cpe + s_shift[nq]);
+  const unsigned qa[4] = {q4.x, q4.y, q4.z, q4.w};
+  float cq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < (NQ > 0 && NQ <= 4 ? NQ : 1); ++k) cq[k] = channel_factor(__uint_as_float(qa[k]), cpm, cpe, s_shift[k]);
+  H[0] = g;
+  H[1] = make_uint4(m.x, __float_as_uint(cw), o.x, o.y);
+  H[2] = make_uint4(o.z, pack, __float_as_uint(inv_small(nc)), __float_as_uint(inv_small(nb * nc)));
+  H[3] = make_uint4(__float_as_uint(cq[0]), __float_as_uint(cq[1]), __float_as_uint(cq[2]), __float_as_uint(cq[3]));
+}
+
+// The small pairs of a staged chunk (lanes set in smask; lane j holds pair
+// j's cell count nj), packed: cell t of the concatenation belongs to the
+// first pair whose inclusive count exceeds t.  Per cell the axis terms are
+// formed directly with axis_sq, the same operations the tables hold, so u
+// and the weight equal those of the renormalisation pass.  Cells of two
+// pairs may meet in one step; the accumulation is atomic.
+template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
+__device__ __forceinline__ void deposit_small(const uint4* R, unsigned smask, int nj, const int* s_shift, int nq,
+                                              int TV, uint4 (*hdr)[4], float* hi, float* lo, unsigned long long* fx,
+                                              int lane) {
+  const unsigned full = 0xffffffffu;
+  const bool mine = (smask >> lane) & 1u;
+  if (mine) small_header<DIMS, NQ>(R + lane * kPairRecWords, s_shift, nq, hdr[lane]);
+  int incl = mine ? nj : 0;  // inclusive scan of the small pairs' cell counts
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(full, incl, 31);
+  __syncwarp();
+  for (int base = 0; base < total; base += 32) {
+    const int t = base + lane;
+    int j = 0;  // the first pair (lane) whose inclusive count exceeds t
+#pragma unroll
+    for (int step = 8; step > 0; step >>= 1) {
+      const int v = __shfl_sync(full, incl, j + step - 1);
+      if (v <= t) j += step;
+    }
+    const int start = __shfl_sync(full, incl - (mine ? nj : 0), j);
+    if (t >= total) continue;
+    const uint4 g = hdr[j][0], h1 = hdr[j][1], h2 = hdr[j][2];
+    const int e = t - start;
+    const int bc = DIMS == 3 ? fdiv(e, __uint_as_float(h2.z)) : e;
+    const int c = DIMS == 3 ? e - bc * (int)(((h2.y >> 20) & 31u) + 1) : 0;
+    const int nb = (int)((h2.y >> 15) & 31u) + 1;
+    const int a = fdiv(e, __uint_as_float(h2.w));
+    const int b = bc - a * nb;
+    const float h = __uint_as_float(g.w);
+    const float2 ex = axis_sq(__uint_as_float(g.x), h, (int)h1.z + a);
+    const float2 ey = axis_sq(__uint_as_float(g.y), h, (int)h1.w + b);
+    const float2 ez = DIMS == 3 ? axis_sq(__uint_as_float(g.z), h, (int)h2.x + c) : make_float2(0.0f, 1.0f);
+    const float u = u_of((ex.x + ey.x) + ez.x, __uint_as_float(h1.x));
+    if (u <= 1.0f) {
+      const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
+      const int li = (int)(h2.y & 1023u) + (a * TY + b) * TZ + c;
+      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, gw * __uint_as_float(h1.y));
+      const uint4 q4 = hdr[j][3];
+      const float cq[4] = {__uint_as_float(q4.x), __uint_as_float(q4.y), __uint_as_float(q4.z), __uint_as_float(q4.w)};
+#pragma unroll
+      for (int k = 0; k < (NQ > 0 && NQ <= 4 ? NQ : 1); ++k) acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li, gw * cq[k]);
+    }
+  }
+  __syncwarp();  // the headers are rewritten for the next chunk
 }
 
 template <int DIMS, int KERN, int NQ, int TX, int TY, int TZ, bool DET>
@@ -1246,9 +1313,32 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       parity ^= 1u << b;
       const int s0 = f0 + c * kStage;
       const int cnt = f1 - s0 < kStage ? f1 - s0 : kStage;
+      const uint4* R = stage[b];
+      unsigned smask = 0;
+      if (NQ > 0 && NQ <= 4) {  // pairs of at most kSmallCells cells go packed
+        int nj = 0;
+        if (lane < cnt) {
+          const unsigned pk = R[lane * kPairRecWords + 1].w;
+          nj = (int)(((pk >> 10) & 31u) + 1) * (int)(((pk >> 15) & 31u) + 1) *
+               (DIMS == 3 ? (int)(((pk >> 20) & 31u) + 1) : 1);
+        }
+        smask = __ballot_sync(0xffffffffu, lane < cnt && nj <= kSmallCells);
+        if (smask) {
+#define SPHG_SMALL(K) \
+  deposit_small<DIMS, K, NQ, TY, TZ, DET>(R, smask, nj, s_shift, nq, TV, sh.small[warp & 7], hi, lo, fx, lane)
+          if (KERN >= 0) SPHG_SMALL(KERN >= 0 ? KERN : 0);
+          else if (A.kern == 0) SPHG_SMALL(0);
+          else if (A.kern == 1) SPHG_SMALL(1);
+          else if (A.kern == 2) SPHG_SMALL(2);
+          else if (A.kern == 3) SPHG_SMALL(3);
+          else SPHG_SMALL(4);
+#undef SPHG_SMALL
+        }
+      }
       for (int j = 0; j < cnt; ++j)
-        deposit_pair32<DIMS, KERN, NQ, TY, TZ, DET>(A, stage[b] + j * kPairRecWords, nq, TV, s_shift, tab, hi, lo,
-                                                    fx, lane);
+        if (!((smask >> j) & 1u))
+          deposit_pair32<DIMS, KERN, NQ, TY, TZ, DET>(A, R + j * kPairRecWords, nq, TV, s_shift, tab, hi, lo, fx,
+                                                      lane);
       __syncwarp();
       if (lane == 0) fence_proxy_async_smem();  // this buffer's reads before its next bulk copy
       b ^= 1;
