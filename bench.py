@@ -204,6 +204,12 @@ def bench_gpu(args):
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
+    if args.workload == "projection_2d":
+        import __graft_entry__ as graft
+        out = bench_config1(graft.load_package(), dev, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return 0
     if args.workload == "healpix":
         import __graft_entry__ as graft
         out = bench_healpix(graft.load_package(), dev, args.steps, args.warmup, n=args.healpix_particles)
@@ -212,7 +218,8 @@ def bench_gpu(args):
         return 0
     if args.workload == "large_hdr":
         import __graft_entry__ as graft
-        out = bench_large(graft.load_package(), dev, args.steps, args.warmup)
+        out = bench_large(graft.load_package(), dev, args.steps, args.warmup, n=args.large_particles,
+                          npix=args.large_npix, seed_grid=512 if args.large_particles >= 2 ** 25 else 128)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return 0
@@ -798,15 +805,16 @@ def _onchip_ceiling(L, ctx, _lib, value, other, det):
     one quantity + the weight = 2 channel additions per deposit), from the
     library's conflict-free microbenchmark, and the fraction reached."""
     names = {0: "fp32_atomic_with_return", 1: "fp32_atomic_no_return", 2: "int64_atomic",
-             3: "fp32_compensated_add"}
+             3: "fp32_compensated_add_two_atomics", 4: "fp32_compensated_pair_cas",
+             5: "int64_fixed_point_two_u32_atomics"}
     rates = {}
     for kind, nm in names.items():
         r = C.c_double()
         _lib.check(L.sphg_probe_smem_rate(ctx.handle, kind, C.byref(r)), ctx.handle)
         rates[nm] = r.value
     chans = 2
-    ceil_c = rates["fp32_compensated_add"] / chans
-    ceil_d = rates["int64_atomic"] / chans
+    ceil_c = rates["fp32_compensated_add_two_atomics"] / chans  # the FP32C deposit's accumulation
+    ceil_d = rates["int64_fixed_point_two_u32_atomics"] / chans  # the deterministic deposit's
     v_c = value if not det else (other or {}).get("value")
     v_d = value if det else (other or {}).get("value")
     return {"smem_additions_per_s": rates, "channel_additions_per_deposit": chans,
@@ -870,9 +878,13 @@ def main():
     ap.add_argument("--batched-maps", type=int, default=96,
                     help="maps in the batched workload (smaller for profiler captures)")
     ap.add_argument("--workload", default="clumps_3d",
-                    choices=["clumps_3d", "large_hdr", "healpix", "differentiable"],
+                    choices=["clumps_3d", "large_hdr", "healpix", "differentiable", "projection_2d"],
                     help="large_hdr: the large-particle projection (2^27 particles, 4096^2), "
                          "FP32C and deterministic against plain FP64 with the error map")
+    ap.add_argument("--large-particles", type=int, default=2 ** 27,
+                    help="particles of the large-particle workload (smaller for profiler captures)")
+    ap.add_argument("--large-npix", type=int, default=4096,
+                    help="Npixels of the large-particle workload")
     ap.add_argument("--healpix-particles", type=int, default=2 ** 20,
                     help="particles of the all-sky workload (smaller for profiler captures)")
     ap.add_argument("--batched-tuning", default=None,

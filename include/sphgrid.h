@@ -264,10 +264,14 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
 /* Measurement only (no counterpart in the reference): the rate, in additions
  * per second over the whole GPU, of the shared-memory accumulation step of
  * the tile deposit -- kind 0: FP32 atomic add with its old value used;
- * 1: FP32 atomic add without return; 2: int64 atomic add (deterministic
- * mode); 3: the compensated FP32 add (atomic add, TwoSum, error term into a
- * second accumulator).  Conflict-free addresses: an upper bound, not a
- * deposit rate.  Synchronous; allocates a few bytes of device memory. */
+ * 1: FP32 atomic add without return; 2: int64 atomic add; 3: the FP32C
+ * deposit's compensated add (atomic add, TwoSum, error term into a second
+ * accumulator); 4: the same compensated add of an adjacent (hi, lo) pair by
+ * one 64-bit compare-and-swap (an alternative, not used); 5: the
+ * deterministic deposit's int64 fixed-point add as two native 32-bit atomics
+ * with a carry.
+ * Conflict-free addresses: an upper bound, not a deposit rate.  Synchronous;
+ * allocates a few bytes of device memory. */
 int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);
 
 /* Per-particle state and integer pixel ranges, from the device code every

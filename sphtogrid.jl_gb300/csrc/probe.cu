@@ -6,9 +6,12 @@
 //
 // Kinds: 0 FP32 atomic add whose old value is used (the first half of the
 // compensated add); 1 FP32 atomic add without return; 2 int64 atomic add
-// (deterministic mode); 3 the whole compensated add of the FP32C method
-// (atomic add with return, TwoSum, error term added to the second
-// accumulator).  Lanes of a warp address distinct banks, as the cells of one
+// (deterministic mode, as 64-bit atomics); 3 the compensated add with two
+// FP32 atomics (atomic add with return, TwoSum, error term added to a second
+// accumulator, the FP32C deposit's); 4 the same compensated add of an
+// adjacent (hi, lo) pair by one 64-bit compare-and-swap (not used by the
+// deposit); 5 the deterministic deposit's int64 fixed-point add as two native
+// 32-bit atomics with a carry.  Lanes of a warp address distinct banks, as the cells of one
 // deposit iteration do, so the figure is the conflict-free ceiling.
 #include <cuda_runtime.h>
 
@@ -41,8 +44,17 @@ __global__ void __launch_bounds__(256, 4) k_probe_smem(float* sink) {
       atomicAdd(&hi[idx], v);
     } else if (KIND == 2) {
       atomicAdd(&fx[idx], (unsigned long long)(i + threadIdx.x));
-    } else {
+    } else if (KIND == 3) {
       acc_twosum(&hi[idx], &lo[idx], v);
+    } else if (KIND == 4) {
+      acc_pair(reinterpret_cast<float2*>(raw) + idx, v);
+    } else {  // int64 fixed point as two native 32-bit words with a carry
+      unsigned* w = reinterpret_cast<unsigned*>(raw);
+      const unsigned long long x = (unsigned long long)(long long)(v * 1.0e9f);
+      const unsigned xl = (unsigned)x;
+      const unsigned old = atomicAdd(&w[idx], xl);
+      const unsigned xh = (unsigned)(x >> 32) + (old + xl < old ? 1u : 0u);
+      if (xh != 0u) atomicAdd(&w[kProbeCells + idx], xh);
     }
     v = v * 1.0001f;
   }
@@ -71,7 +83,9 @@ cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_p
       case 0: launch_probe<0>(grid, sink, s); break;
       case 1: launch_probe<1>(grid, sink, s); break;
       case 2: launch_probe<2>(grid, sink, s); break;
-      default: launch_probe<3>(grid, sink, s); break;
+      case 3: launch_probe<3>(grid, sink, s); break;
+      case 4: launch_probe<4>(grid, sink, s); break;
+      default: launch_probe<5>(grid, sink, s); break;
     }
     cudaEventRecord(e1, s);
     e = cudaEventSynchronize(e1);

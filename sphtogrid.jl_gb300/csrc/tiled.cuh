@@ -165,6 +165,29 @@ __device__ __forceinline__ void acc_twosum(float* hi, float* lo, float v) {
   if (e != 0.0f) atomicAdd(lo, e);
 }
 
+// The same compensated accumulation into an adjacent (hi, lo) pair with one
+// 64-bit compare-and-swap per attempt: the pair is read, v is added to hi
+// with TwoSum and its error to lo, and both words are swapped in together
+// if the pair is unchanged (else the attempt repeats on the pair it found;
+// some thread's swap succeeds on every round, so the loop ends).  One loop
+// per channel instead of the two FP32 atomics' loops, but measured slower in
+// the deposit (3D 7.33 against 6.97 ms, 96-map batch 97.6 against 80.5 ms);
+// kept for the accumulation microbenchmark (sphg_probe_smem_rate kind 4).
+__device__ __forceinline__ void acc_pair(float2* p, float v) {
+  unsigned long long* a = reinterpret_cast<unsigned long long*>(p);
+  unsigned long long seen = *a;
+  for (;;) {
+    const float hi = __uint_as_float((unsigned)seen), lo = __uint_as_float((unsigned)(seen >> 32));
+    float s, e;
+    two_sum(hi, v, s, e);
+    const unsigned long long want =
+        (unsigned long long)__float_as_uint(s) | ((unsigned long long)__float_as_uint(lo + e) << 32);
+    const unsigned long long was = atomicCAS(a, seen, want);
+    if (was == seen) return;
+    seen = was;
+  }
+}
+
 
 // A record is redone in FP64 when every pixel centre is near or beyond the
 // kernel edge (FP32 cancellation in 1 - u), when its FP32 sum is 0 (the

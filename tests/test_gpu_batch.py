@@ -65,10 +65,23 @@ def test_batch_matches_single_maps(gpu, oracle):
         assert got.shape == ref.shape
         assert rel_linf(got, ref, 1e-9) <= 1e-6, i
         opar = oracle.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=d["P"])
-        _, info = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["m"], d["rho"], d["q"],
-                                     d["w"], param=opar, kernel=d["kernel"], dimensions=d["dims"])
+        oref, info = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["m"], d["rho"], d["q"],
+                                        d["w"], param=opar, kernel=d["kernel"], dimensions=d["dims"])
         assert stats[i]["deposits"] == info["deposits"]
         assert stats[i]["n_launches"] == 6
+        # the batched map itself against the oracle, on the pixels carrying
+        # weight (W >= 1e-6 max W), relative to each pixel's value (q > 0)
+        raw, _ = oracle.sph_mapping(d["pos"].copy(order="F"), d["hsml"], d["m"], d["rho"], d["q"], d["w"],
+                                    param=opar, kernel=d["kernel"], dimensions=d["dims"],
+                                    return_both_maps=True, raw3d=True)
+        P = d["P"]
+        W = raw[:, -1]
+        keep = W >= 1e-6 * W.max() if W.max() > 0 else np.zeros_like(W, bool)
+        keep = keep.reshape(P, P, 1) if d["dims"] == 2 else keep.reshape(P, P, P).transpose(2, 1, 0)
+        keep = np.broadcast_to(keep, got.shape)
+        oref = np.asarray(oref).reshape(got.shape)
+        if keep.any():
+            assert (np.abs(got - oref)[keep] / np.abs(oref)[keep]).max() <= 1e-5, i
     b.close()
 
 

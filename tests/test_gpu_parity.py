@@ -419,9 +419,10 @@ def test_fp32c_uniform_2d_workload_full_size(gpu, oracle):
     assert rel_linf(img, ref, FLOOR) <= TOL["fp32c"]
 
 
-def test_fp32c_clumps_3d_full_size(gpu):
-    """3D workload at full size: FP32C against the plain FP64 GPU method (which
-    itself matches the oracle to 1e-11), and mass conservation."""
+def test_fp32c_clumps_3d_full_size(gpu, oracle):
+    """3D workload at full size: FP32C against the oracle (all host threads)
+    and against the plain FP64 GPU method, and mass conservation."""
+    import os
     from sphtogrid_gb300 import synth
     d = synth.clumps_3d()
     par = gpu.mappingParameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=256)
@@ -433,6 +434,11 @@ def test_fp32c_clumps_3d_full_size(gpu):
     assert sa["deposits"] == sb["deposits"] and sa["n_mapped"] == sb["n_mapped"]
     assert rel_linf(a, b, FLOOR) <= TOL["fp32c"]
     assert math.isclose(sa["grid_mass"], sb["grid_mass"], rel_tol=1e-5)
+    opar = oracle.mapping_parameters(x_lim=[0, 1], y_lim=[0, 1], z_lim=[0, 1], Npixels=256)
+    ref, info = oracle.sph_mapping(d["pos"].copy(order="F"), *args, param=opar, kernel="wendlandc6",
+                                   dimensions=3, nthreads=os.cpu_count() or 1)
+    assert info["deposits"] == sa["deposits"]
+    assert rel_linf(a, ref, FLOOR) <= TOL["fp32c"]
 
 
 # ------------------------------------------------------- deterministic mode
