@@ -315,6 +315,9 @@ __device__ __forceinline__ void prep_bcast(const DevParticles& pt, const DevMapP
 }
 
 // Compensated butterfly reduction of (s, comp) and min of umin over a warp.
+// u is never negative, so the order of its bit patterns as unsigned
+// integers is the order of the values: one warp-wide integer min instead of
+// five shuffle rounds.
 __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& umin) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -324,8 +327,8 @@ __device__ __forceinline__ void warp_reduce_comp(float& s, float& comp, float& u
     two_sum(s, so, t, e);
     s = t;
     comp = comp + co + e;
-    umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
   }
+  umin = __uint_as_float(__reduce_min_sync(0xffffffffu, __float_as_uint(umin)));
 }
 
 // Stores the finished weight factor cpv of record r (FP64, and as FP32
@@ -1219,7 +1222,8 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // after an overflow of the pair list the lists are incomplete: deposit
   // nothing (the host grows the list and maps again); nor after a staging
   // copy timed out (the call fails)
-  const bool overflow = (A.st->flags & (kFlagOverflow | kFlagTimeout)) != 0;
+  // (read from L2: a timeout raised by an earlier tile of this CTA must be seen)
+  const bool overflow = (__ldcg(&A.st->flags) & (kFlagOverflow | kFlagTimeout)) != 0;
   // the tile's slots hold the pairs the renormalisation pass kept: FP32
   // pairs from the start, FP64 pairs from the end
   const long long p0 = A.tile_start[t], pe = A.tile_start[t + 1];
