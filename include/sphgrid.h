@@ -274,6 +274,13 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
  * allocates a few bytes of device memory. */
 int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);
 
+/* Diagnostics only (no counterpart in the reference): the tile deposit's
+ * bounded wait for a bulk copy, run on a barrier that no copy completes.
+ * The wait gives up after `polls` polls (1..2^20) and *timed_out is set to 1
+ * -- the path that turns a copy that never lands into SPHG_ERR_TIMEOUT
+ * instead of a hang.  Synchronous; allocates a few bytes of device memory. */
+int sphg_probe_wait_timeout(sphg_context *ctx, int32_t polls, int32_t *timed_out);
+
 /* Per-particle state and integer pixel ranges, from the device code every
  * map runs (center_particles and filter_particles_in_image,
  * filter_shift.jl:6-58; the quantity skip, cic_2D.jl:154-168;

@@ -807,6 +807,17 @@ int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n
   return SPHG_OK;
 }
 
+int sphg_probe_wait_timeout(sphg_context* ctx, int32_t polls, int32_t* timed_out) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!timed_out || polls < 1 || polls > (1 << 20)) return fail(ctx, SPHG_ERR_ARG, "polls must be in 1..2^20");
+  DeviceGuard g(ctx->device);
+  int t = 0;
+  CK(sphg::probe_wait_timeout(polls, ctx->stream, &t));
+  *timed_out = t;
+  return SPHG_OK;
+}
+
 int sphg_probe_smem_rate(sphg_context* ctx, int kind, double* ops_per_s) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
   std::lock_guard<std::mutex> lk(ctx->mu);

@@ -17,6 +17,7 @@
 
 #include "internal.h"
 #include "tiled.cuh"
+#include "tiled_kernels.cuh"
 
 namespace sphg {
 namespace {
@@ -67,7 +68,35 @@ void launch_probe(int grid, float* sink, cudaStream_t s) {
   k_probe_smem<KIND><<<grid, 256, 0, s>>>(sink);
 }
 
+// The deposit's bounded staging wait on a barrier that no bulk copy
+// completes (no copy is issued): the wait gives up after `polls` polls and
+// the kernel records that, as the deposit records a timeout.
+__global__ void __launch_bounds__(32) k_probe_wait(int polls, int* timed_out) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    tiled_detail::mbar_init(&bar, 1);
+    tiled_detail::fence_proxy_async_smem();
+    tiled_detail::fence_mbar_init();
+  }
+  __syncwarp();
+  const bool done = tiled_detail::mbar_wait_warp(&bar, 0u, polls);
+  if (threadIdx.x == 0) *timed_out = done ? 0 : 1;
+}
+
 }  // namespace
+
+cudaError_t probe_wait_timeout(int polls, cudaStream_t s, int* timed_out) {
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e == cudaSuccess) {
+    k_probe_wait<<<1, 32, 0, s>>>(polls, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(timed_out, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFree(d);
+  return e;
+}
 
 cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_per_s) {
   const int grid = num_sms * 4;

@@ -952,9 +952,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return ok != 0;
 }
 // The whole warp waits for the phase of parity `parity` to complete; false
-// when it has not after kSpinLimit polls (warp-uniform).
-__device__ __forceinline__ bool mbar_wait_warp(unsigned long long* bar, unsigned parity) {
-  for (int it = 0; it < kSpinLimit; ++it)
+// when it has not after `limit` polls (warp-uniform).
+__device__ __forceinline__ bool mbar_wait_warp(unsigned long long* bar, unsigned parity, int limit = kSpinLimit) {
+  for (int it = 0; it < limit; ++it)
     if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
   return false;
 }
