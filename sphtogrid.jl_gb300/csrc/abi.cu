@@ -469,6 +469,7 @@ again:
   mp.L = cpar.len2pix;
   mp.P = P;
   mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
+  sphg::set_lite_params(mp);
 
   cudaEvent_t* ev = opt->profile ? ctx->ev : nullptr;
   int n_launch = 0;
@@ -692,6 +693,7 @@ int sphg_footprints(sphg_context* ctx, const sphg_params* par, const sphg_option
   mp.L = cpar.len2pix;
   mp.P = P;
   mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
+  sphg::set_lite_params(mp);
   CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(sphg::DevStatus), s));
   if (n > 0) {
     sphg::launch_footprints(d, mp, (long long*)ranges, (signed char*)state, ctx->d_status, ctx->num_sms, s);

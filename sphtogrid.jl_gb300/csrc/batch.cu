@@ -413,6 +413,7 @@ int build_plan(sphg_batch* b) {
     mp.L = M.cpar.len2pix;
     mp.P = P;
     mp.sigma = kernel_sigma(D.opt.kernel, D.opt.kernel_dim);
+    set_lite_params(mp);
     A.mp_re = mp;
     A.kern = D.opt.kernel;
     A.large_cells = p.large_cells;

@@ -5,6 +5,7 @@
 // Wendland C4/C6/C8 functions, all with compact support u = r/h in [0, 1].
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -92,7 +93,29 @@ struct DevMapParams {
   double L;               // len2pix
   int64_t P;              // Npixels
   double sigma;           // kernel normalisation
+  // Single-precision constants of prep_particle_lite, set on the host by
+  // set_lite_params; lite = 0 leaves every particle to prep_particle_fp64.
+  float lo_f[3] = {0.0f, 0.0f, 0.0f};  // lo rounded up to a float
+  float hi_f[3] = {0.0f, 0.0f, 0.0f};  // hi rounded down to a float
+  float L_hi = 0.0f, L_lo = 0.0f;      // L = L_hi + L_lo to about 2^-48 of L
+  int lite = 0;
 };
+
+// Fills the constants of prep_particle_lite from the FP64 parameters.  A
+// float v satisfies lo_f <= v <= hi_f exactly when (double)v satisfies the
+// reference's lo <= v <= hi (NaN bounds fail both).
+inline void set_lite_params(DevMapParams& mp) {
+  for (int d = 0; d < 3; ++d) {
+    float lo = (float)mp.lo[d], hi = (float)mp.hi[d];
+    if ((double)lo < mp.lo[d]) lo = std::nextafter(lo, INFINITY);
+    if ((double)hi > mp.hi[d]) hi = std::nextafter(hi, -INFINITY);
+    mp.lo_f[d] = lo;
+    mp.hi_f[d] = hi;
+  }
+  mp.L_hi = (float)mp.L;
+  mp.L_lo = (float)(mp.L - (double)mp.L_hi);
+  mp.lite = std::isfinite(mp.L_hi) && std::isfinite(mp.L_lo) && mp.L_hi != 0.0f && mp.P > 0 && mp.P < (1 << 22);
+}
 
 // Device-side status and statistics of one map call.
 struct DevStatus {
@@ -244,6 +267,160 @@ __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const 
     if (o->hi[d] < o->lo[d]) o->hi[d] = o->lo[d] - 1;
   }
   return kPrepMapped;
+}
+
+// One particle as the FP32 method's first pass needs it.
+struct PrepLite {
+  int64_t lo[3], hi[3];     // pix_index_min_max per axis, as PrepFP64
+  float g[4];               // x - lo[0], y - lo[1], z - lo[2] and hsml, pixel units
+  double m_in, rho_in, wgt, hsml;
+  bool scalar_zero;
+};
+
+// Error-free a + b == s + e (Knuth's TwoSum; no FMA contraction here).
+__device__ __forceinline__ void prep_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// floor(xh + xl + hh + hl) from two unevaluated float sums (the pixel
+// coordinate and +-hsml in pixels); false when the sum lies within `delta`
+// of an integer.  s1 - floor(s1) is exact for |s1| < 2^23, so the only
+// roundings are those of the small terms and of the final sum (at most
+// 2^-23 absolute, as r < 2).
+__device__ __forceinline__ bool floor_lite(float xh, float xl, float hh, float hl, float delta, int64_t* out) {
+  float s1, e1;
+  prep_two_sum(xh, hh, s1, e1);
+  const float a = floorf(s1);
+  const float r = (s1 - a) + ((e1 + xl) + hl);
+  const float k = floorf(r);
+  const float fr = r - k;
+  if (!(fr >= delta && fr <= 1.0f - delta)) return false;
+  *out = (int64_t)(a + k);
+  return true;
+}
+
+// The centring, filter, quantity skip and pixel ranges of prep_particle_fp64
+// for FP32 inputs, with the FP64 pipe used only for the centring: the same
+// state, the same centred positions and the same integer ranges, bit for bit.
+//  - The filter compares the centred float against the box rounded inwards
+//    to floats (set_lite_params), which is exact.
+//  - pix_index_min_max takes floor(x -+ h) with x = c L + P/2 and h = hsml L
+//    (cic_shared.jl:46-52, 85-99).  Here x and h L are unevaluated sums of
+//    two floats (L = L_hi + L_lo; products split exactly by FMA), accurate
+//    to about 2^-44 of M = |c L| + P/2 + |h L|; the reference's four FP64
+//    roundings move its value by under 2^-50 M.  When the two-float value
+//    is farther than delta = 2^-21 + 2^-36 M from every integer, the floor
+//    of the reference's FP64 value is the floor of the two-float one.
+//  - Otherwise (a value that close to an integer, M >= 2^22, non-finite
+//    values, FP64 or rotated inputs) the particle is prepared by
+//    prep_particle_fp64 from its untouched inputs.
+// The record's FP32 offsets x - lo and hsml are rounded from the two-float
+// sums (within an FP32 rounding of the FP64-derived values).
+template <int DIMS>
+__device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const DevMapParams& mp, int64_t p,
+                                                  bool store_pos, PrepLite* o) {
+  bool fp64 = !mp.lite || pt.pos_dtype != 0 || pt.attr_dtype != 0 || pt.xform == 2;
+  int state = kPrepMapped;
+  if (!fp64) {
+    float c[3];
+    int64_t off[3];
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      off[d] = p * pt.sp + (pt.xform == 1 ? pt.perm[d] : d) * pt.sc;
+      float v = __ldg((const float*)pt.pos + off[d]);
+      if (mp.center_mode != 0) {
+        v = __double2float_rn((double)v - mp.cen[d]);
+        if (mp.periodic && fabs((double)v) > mp.boxsize / 2) {
+          const double vd = v;
+          v = __double2float_rn(vd > 0 ? vd - mp.boxsize / 2 : vd + mp.boxsize / 2);
+        }
+      }
+      c[d] = v;
+      if (mp.filter && !(mp.lo_f[d] <= v && v <= mp.hi_f[d])) in = false;
+    }
+    if (!in) {
+      state = kPrepSkip;
+    } else {
+      bool allzero = true;
+      for (int k = 0; k < pt.nq; ++k)
+        if (__ldg((const float*)pt.q + p * pt.qsp + k * pt.qsk) != 0.0f) allzero = false;
+      if (allzero && !mp.calc_mean) {
+        state = kPrepZeroQ;
+      } else {
+        o->scalar_zero = (pt.nq > 1) && allzero;
+        const float hin = __ldg((const float*)pt.hsml + p);
+        const float halfP = 0.5f * (float)mp.P;
+        const float hh = hin * mp.L_hi;
+        const float hl = fmaf(hin, mp.L_hi, -hh) + hin * mp.L_lo;
+        o->g[3] = hh + hl;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          if (d >= DIMS) {
+            o->lo[d] = 0;
+            o->hi[d] = 0;
+            o->g[d] = 0.0f;
+            continue;
+          }
+          const float ph = c[d] * mp.L_hi;
+          const float pe = fmaf(c[d], mp.L_hi, -ph);
+          float xh, e0;
+          prep_two_sum(ph, halfP, xh, e0);
+          const float xl = (e0 + pe) + c[d] * mp.L_lo;
+          const float M = (fabsf(ph) + halfP) + fabsf(hh) + 1.0f;
+          int64_t a, b;
+          if (!(M < 0x1p22f)) {
+            fp64 = true;
+            break;
+          }
+          const float delta = 0x1p-21f + M * 0x1p-36f;
+          if (!floor_lite(xh, xl, -hh, -hl, delta, &a) || !floor_lite(xh, xl, hh, hl, delta, &b)) {
+            fp64 = true;
+            break;
+          }
+          const int64_t P = mp.P;
+          o->lo[d] = a > 0 ? a : 0;
+          o->hi[d] = b < P - 1 ? b : P - 1;
+          if (o->hi[d] < o->lo[d]) o->hi[d] = o->lo[d] - 1;
+          float g1, g2;
+          prep_two_sum(xh, -(float)o->lo[d], g1, g2);
+          o->g[d] = g1 + (g2 + xl);
+        }
+        if (!fp64) {
+          o->m_in = (double)__ldg((const float*)pt.mass + p);
+          o->rho_in = (double)__ldg((const float*)pt.rho + p);
+          o->wgt = (double)__ldg((const float*)pt.w + p);
+          o->hsml = (double)o->g[3];
+        }
+      }
+    }
+    if (!fp64) {
+      if (mp.center_mode == 1 && store_pos && pt.xform == 0)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ((float*)pt.pos)[off[d]] = c[d];
+      return state;
+    }
+  }
+  PrepFP64 q;
+  state = prep_particle_fp64<DIMS, false>(pt, mp, p, store_pos, &q);
+  if (state == kPrepMapped) {
+    const double xs[3] = {q.x, q.y, q.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o->lo[d] = q.lo[d];
+      o->hi[d] = q.hi[d];
+      o->g[d] = d < DIMS ? __double2float_rn(xs[d] - (double)q.lo[d]) : 0.0f;
+    }
+    o->g[3] = __double2float_rn(q.hsml);
+    o->m_in = q.m_in;
+    o->rho_in = q.rho_in;
+    o->wgt = q.wgt;
+    o->hsml = q.hsml;
+    o->scalar_zero = q.scalar_zero;
+  }
+  return state;
 }
 
 // Offset of a pixel centre and the overlap of [x - h, x + h] with pixel i

@@ -222,6 +222,7 @@ int sphg_map_noalloc(const sphg_params* par, const sphg_options* opt, const sphg
   mp.L = cpar.len2pix;
   mp.P = P;
   mp.sigma = kernel_sigma(opt->kernel, opt->kernel_dim);
+  set_lite_params(mp);
 
   DevStatus* d_status = (DevStatus*)(ws + o_stat);
   ta.pt = d;

@@ -209,16 +209,17 @@ __global__ void __launch_bounds__(256) k_accumulate_finite(const double* __restr
   }
 }
 
-// Per-particle state and integer pixel ranges (sphg_footprints): the same
-// centring, filter, quantity skip and pix_index_min_max as every mapping
-// kernel (prep_particle_fp64).
+// Per-particle state and integer pixel ranges (sphg_footprints): the
+// centring, filter, quantity skip and pix_index_min_max of the FP32 method's
+// first pass (prep_particle_lite, which hands particles it cannot decide in
+// FP32 to prep_particle_fp64, the plain method's preparation).
 template <int DIMS>
 __global__ void __launch_bounds__(256) k_footprints(DevParticles pt, DevMapParams mp, long long* rng,
                                                     signed char* state, DevStatus* st) {
   unsigned flags = 0;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < pt.n; p += (int64_t)gridDim.x * blockDim.x) {
-    PrepFP64 q;
-    const int s = prep_particle_fp64<DIMS, false>(pt, mp, p, false, &q);
+    PrepLite q;
+    const int s = prep_particle_lite<DIMS>(pt, mp, p, false, &q);
     signed char code = 0;
     long long r[6] = {0, 0, 0, 0, 0, 0};
     if (s == kPrepMapped) {

@@ -24,9 +24,9 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
   unsigned flags = 0;
   for (int64_t base = base0; base < A.pt.n; base += stride) {
     const int64_t p = base + threadIdx.x;
-    PrepFP64 q;
+    PrepLite q;
     int state = kPrepSkip;
-    if (p < A.pt.n) state = prep_particle_fp64<DIMS, false>(A.pt, A.mp, p, true, &q);
+    if (p < A.pt.n) state = prep_particle_lite<DIMS>(A.pt, A.mp, p, true, &q);
     if (state == kPrepNonFinite) flags |= kFlagNonFinite;
     int ni = 0, nj = 0, nk = 0;
     if (state == kPrepMapped) {
@@ -51,9 +51,7 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
       const int i0 = (int)q.lo[0], j0 = (int)q.lo[1], k0 = (int)q.lo[2];
       A.box[r] = make_int4(i0, j0, k0, 0);
       A.dimv[r] = make_int4(ni, nj, nk, (int)p);
-      A.geo[r] = make_float4(__double2float_rn(q.x - (double)i0), __double2float_rn(q.y - (double)j0),
-                             DIMS == 3 ? __double2float_rn(q.z - (double)k0) : 0.0f,
-                             __double2float_rn(q.hsml));
+      A.geo[r] = make_float4(q.g[0], q.g[1], q.g[2], q.g[3]);
       // weight factor numerator, area*w*dz (cic_2D.jl:187-188) = w m / rho_pix
       // or vol*w*L (cic_3D.jl:168-169) = w m L / rho_pix, with
       // rho_pix = rho / L^3; FP32 accuracy suffices here (the FP32 method

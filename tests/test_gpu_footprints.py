@@ -63,7 +63,10 @@ def test_footprints_uniform_2d_full(gpu, oracle):
 def test_footprints_edges(gpu, oracle, dims, P, dtype):
     """Particles on the image boundaries and pixel edges, far outside it,
     with tiny, zero and huge smoothing lengths, and with all quantities zero
-    (skipped unless calc_mean)."""
+    (skipped unless calc_mean).  Pixel-edge particles whose x -+ h falls on
+    an integer pixel coordinate, or one rounding step beside it, and
+    smoothing lengths beyond 2^22 pixels are the cases the FP32 range
+    computation hands to FP64."""
     rng = np.random.default_rng(3)
     n = 6000
     pos = rng.uniform(-0.2, 1.2, (3, n))
@@ -72,8 +75,13 @@ def test_footprints_edges(gpu, oracle, dims, P, dtype):
     pos[0, k:2 * k] = 0.0
     pos[1, 2 * k:3 * k] = 1.0
     hsml = np.exp(rng.uniform(np.log(1e-4), np.log(2.0), n))
+    h = k // 3
+    hsml[:h] = rng.integers(0, 9, h) / P  # x -+ h on a pixel edge
+    hsml[h:2 * h] = np.nextafter(hsml[:h].astype(dtype), np.array(np.inf, dtype)).astype(np.float64)
+    hsml[2 * h:3 * h] = np.nextafter(hsml[:h].astype(dtype), np.array(-np.inf, dtype)).astype(np.float64)
     hsml[3 * k:3 * k + 50] = 0.0
     hsml[3 * k + 50:3 * k + 100] = 5.0
+    hsml[3 * k + 100:3 * k + 120] = 1e7
     q = rng.uniform(0.5, 2.0, n)
     q[4 * k:4 * k + 300] = 0.0
     args = (np.asfortranarray(pos.astype(dtype)), hsml.astype(dtype), q.astype(dtype), dims, P)
