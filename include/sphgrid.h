@@ -291,7 +291,8 @@ int sphg_probe_wait_timeout(sphg_context *ctx, int32_t polls, int32_t *timed_out
  * {iMin, iMax, jMin, jMax, kMin, kMax} of a mapped particle (zeros
  * otherwise; the third axis is 0 0 in 2D; an empty range has max = min - 1).
  * Device memory only; the positions are read, never written
- * (SPHG_CENTER_INPLACE is taken as READONLY).  Synchronous. */
+ * (SPHG_CENTER_INPLACE is taken as READONLY).  mass, rho and weights may be
+ * NULL: they do not enter the state or the ranges.  Synchronous. */
 int sphg_footprints(sphg_context *ctx, const sphg_params *par, const sphg_options *opt,
                     const sphg_particles *parts, int64_t *ranges, int8_t *state, void *stream);
 

@@ -669,9 +669,11 @@ int sphg_footprints(sphg_context* ctx, const sphg_params* par, const sphg_option
   d.sp = pt->pos_stride_p;
   d.sc = pt->pos_stride_c;
   d.hsml = pt->hsml;
-  d.mass = pt->mass;
-  d.rho = pt->rho;
-  d.w = pt->weights;
+  // mass, rho and weights do not enter the state or the ranges, but the
+  // preparation reads them for every particle: absent ones alias hsml
+  d.mass = pt->mass ? pt->mass : pt->hsml;
+  d.rho = pt->rho ? pt->rho : pt->hsml;
+  d.w = pt->weights ? pt->weights : pt->hsml;
   d.q = pt->bin_q;
   d.nq = nq;
   d.qsp = pt->q_stride_p;

@@ -56,12 +56,13 @@ __device__ __forceinline__ int find_seg_i(const int* base, int n, int x) {
 
 constexpr int64_t kOneIteration = (int64_t)1 << 62;
 
-__global__ void __launch_bounds__(256) kb_prep(BatchDev B) {
+__global__ void __launch_bounds__(256, 4) kb_prep(BatchDev B) {
   const int m = find_seg_i(B.blk_base, B.n_maps, blockIdx.x);
   const TiledArgs& A = B.maps[m];
   const int64_t base = (int64_t)(blockIdx.x - B.blk_base[m]) * blockDim.x;
-  if (A.mp.dims == 2) prep_count<2>(A, base, kOneIteration);
-  else prep_count<3>(A, base, kOneIteration);
+  __shared__ PrepShared sh;
+  if (A.mp.dims == 2) prep_count<2>(A, base, kOneIteration, sh);
+  else prep_count<3>(A, base, kOneIteration, sh);
 }
 
 __global__ void __launch_bounds__(1024) kb_scan(BatchDev B) {

@@ -99,6 +99,11 @@ struct DevMapParams {
   float hi_f[3] = {0.0f, 0.0f, 0.0f};  // hi rounded down to a float
   float L_hi = 0.0f, L_lo = 0.0f;      // L = L_hi + L_lo to about 2^-48 of L
   int lite = 0;
+  float cen_f[3] = {0.0f, 0.0f, 0.0f};  // cen as floats, used when cen_f_exact
+  int cen_f_exact = 0;                  // every cen[d] is a float
+  float fac_m[3] = {0.0f, 0.0f, 0.0f};  // L, L^3 and sigma as fac_m 2^fac_e,
+  int fac_e[3] = {0, 0, 0};             // fac_m in [0.5, 1]
+  int fac_ok = 0;                       // the three are finite and positive
 };
 
 // Fills the constants of prep_particle_lite from the FP64 parameters.  A
@@ -115,6 +120,22 @@ inline void set_lite_params(DevMapParams& mp) {
   mp.L_hi = (float)mp.L;
   mp.L_lo = (float)(mp.L - (double)mp.L_hi);
   mp.lite = std::isfinite(mp.L_hi) && std::isfinite(mp.L_lo) && mp.L_hi != 0.0f && mp.P > 0 && mp.P < (1 << 22);
+  mp.cen_f_exact = 1;
+  for (int d = 0; d < 3; ++d) {
+    mp.cen_f[d] = (float)mp.cen[d];
+    if (!((double)mp.cen_f[d] == mp.cen[d])) mp.cen_f_exact = 0;
+  }
+  const double fac[3] = {mp.L, mp.L * mp.L * mp.L, mp.sigma};
+  mp.fac_ok = 1;
+  for (int i = 0; i < 3; ++i) {
+    if (!(std::isfinite(fac[i]) && fac[i] > 0.0)) {
+      mp.fac_ok = 0;
+      continue;
+    }
+    int e = 0;
+    mp.fac_m[i] = (float)std::frexp(fac[i], &e);
+    mp.fac_e[i] = e;
+  }
 }
 
 // Device-side status and statistics of one map call.
@@ -274,6 +295,8 @@ struct PrepLite {
   int64_t lo[3], hi[3];     // pix_index_min_max per axis, as PrepFP64
   float g[4];               // x - lo[0], y - lo[1], z - lo[2] and hsml, pixel units
   double m_in, rho_in, wgt, hsml;
+  float m32, rho32, w32;    // the same as read (f32 set: Float32 inputs)
+  bool f32;
   bool scalar_zero;
 };
 
@@ -301,6 +324,32 @@ __device__ __forceinline__ bool floor_lite(float xh, float xl, float hh, float h
   return true;
 }
 
+// prep_particle_lite's FP64 path: prep_particle_fp64, results as PrepLite
+// (out of line: it is the rare path, and inlined it costs the common one
+// registers).
+template <int DIMS>
+__device__ __noinline__ int prep_lite_fp64(const DevParticles& pt, const DevMapParams& mp, int64_t p,
+                                           bool store_pos, PrepLite* o) {
+  PrepFP64 q;
+  const int state = prep_particle_fp64<DIMS, false>(pt, mp, p, store_pos, &q);
+  if (state == kPrepMapped) {
+    const double xs[3] = {q.x, q.y, q.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o->lo[d] = q.lo[d];
+      o->hi[d] = q.hi[d];
+      o->g[d] = d < DIMS ? __double2float_rn(xs[d] - (double)q.lo[d]) : 0.0f;
+    }
+    o->g[3] = __double2float_rn(q.hsml);
+    o->m_in = q.m_in;
+    o->rho_in = q.rho_in;
+    o->wgt = q.wgt;
+    o->hsml = q.hsml;
+    o->scalar_zero = q.scalar_zero;
+  }
+  return state;
+}
+
 // The centring, filter, quantity skip and pixel ranges of prep_particle_fp64
 // for FP32 inputs, with the FP64 pipe used only for the centring: the same
 // state, the same centred positions and the same integer ranges, bit for bit.
@@ -316,23 +365,40 @@ __device__ __forceinline__ bool floor_lite(float xh, float xl, float hh, float h
 //  - Otherwise (a value that close to an integer, M >= 2^22, non-finite
 //    values, FP64 or rotated inputs) the particle is prepared by
 //    prep_particle_fp64 from its untouched inputs.
-// The record's FP32 offsets x - lo and hsml are rounded from the two-float
+//  - The centring is the reference's FP64 subtraction rounded to Float32;
+//    when the centre is a float it is one FP32 subtraction, which is the
+//    same: the difference of two floats is exact in FP64 unless their
+//    exponents differ by more than 29, and then it is within half an FP32
+//    ulp of the larger, far from an FP32 rounding boundary, so rounding it
+//    to FP64 first does not change its FP32 rounding.
+// The particle's inputs are all read first, so the loads overlap.  The
+// record's FP32 offsets x - lo and hsml are rounded from the two-float
 // sums (within an FP32 rounding of the FP64-derived values).
 template <int DIMS>
 __device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const DevMapParams& mp, int64_t p,
                                                   bool store_pos, PrepLite* o) {
   bool fp64 = !mp.lite || pt.pos_dtype != 0 || pt.attr_dtype != 0 || pt.xform == 2;
   int state = kPrepMapped;
+  o->f32 = false;
   if (!fp64) {
     float c[3];
     int64_t off[3];
-    bool in = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       off[d] = p * pt.sp + (pt.xform == 1 ? pt.perm[d] : d) * pt.sc;
-      float v = __ldg((const float*)pt.pos + off[d]);
+      c[d] = __ldg((const float*)pt.pos + off[d]);
+    }
+    const float hin = __ldg((const float*)pt.hsml + p);
+    const float q0 = pt.nq > 0 ? __ldg((const float*)pt.q + p * pt.qsp) : 0.0f;
+    o->m32 = __ldg((const float*)pt.mass + p);
+    o->rho32 = __ldg((const float*)pt.rho + p);
+    o->w32 = __ldg((const float*)pt.w + p);
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      float v = c[d];
       if (mp.center_mode != 0) {
-        v = __double2float_rn((double)v - mp.cen[d]);
+        v = mp.cen_f_exact ? v - mp.cen_f[d] : __double2float_rn((double)v - mp.cen[d]);
         if (mp.periodic && fabs((double)v) > mp.boxsize / 2) {
           const double vd = v;
           v = __double2float_rn(vd > 0 ? vd - mp.boxsize / 2 : vd + mp.boxsize / 2);
@@ -344,14 +410,13 @@ __device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const 
     if (!in) {
       state = kPrepSkip;
     } else {
-      bool allzero = true;
-      for (int k = 0; k < pt.nq; ++k)
+      bool allzero = q0 == 0.0f;
+      for (int k = 1; k < pt.nq; ++k)
         if (__ldg((const float*)pt.q + p * pt.qsp + k * pt.qsk) != 0.0f) allzero = false;
       if (allzero && !mp.calc_mean) {
         state = kPrepZeroQ;
       } else {
         o->scalar_zero = (pt.nq > 1) && allzero;
-        const float hin = __ldg((const float*)pt.hsml + p);
         const float halfP = 0.5f * (float)mp.P;
         const float hh = hin * mp.L_hi;
         const float hl = fmaf(hin, mp.L_hi, -hh) + hin * mp.L_lo;
@@ -389,10 +454,11 @@ __device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const 
           o->g[d] = g1 + (g2 + xl);
         }
         if (!fp64) {
-          o->m_in = (double)__ldg((const float*)pt.mass + p);
-          o->rho_in = (double)__ldg((const float*)pt.rho + p);
-          o->wgt = (double)__ldg((const float*)pt.w + p);
+          o->m_in = (double)o->m32;
+          o->rho_in = (double)o->rho32;
+          o->wgt = (double)o->w32;
           o->hsml = (double)o->g[3];
+          o->f32 = true;
         }
       }
     }
@@ -403,23 +469,9 @@ __device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const 
       return state;
     }
   }
-  PrepFP64 q;
-  state = prep_particle_fp64<DIMS, false>(pt, mp, p, store_pos, &q);
-  if (state == kPrepMapped) {
-    const double xs[3] = {q.x, q.y, q.z};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      o->lo[d] = q.lo[d];
-      o->hi[d] = q.hi[d];
-      o->g[d] = d < DIMS ? __double2float_rn(xs[d] - (double)q.lo[d]) : 0.0f;
-    }
-    o->g[3] = __double2float_rn(q.hsml);
-    o->m_in = q.m_in;
-    o->rho_in = q.rho_in;
-    o->wgt = q.wgt;
-    o->hsml = q.hsml;
-    o->scalar_zero = q.scalar_zero;
-  }
+  PrepLite slow;  // only this path's copy leaves registers
+  state = prep_lite_fp64<DIMS>(pt, mp, p, store_pos, &slow);
+  *o = slow;
   return state;
 }
 

@@ -19,7 +19,8 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 template <int DIMS>
 __global__ void __launch_bounds__(256) k_prep_count(TiledArgs A) {
-  prep_count<DIMS>(A, (int64_t)blockIdx.x * blockDim.x, (int64_t)gridDim.x * blockDim.x);
+  __shared__ PrepShared sh;
+  prep_count<DIMS>(A, (int64_t)blockIdx.x * blockDim.x, (int64_t)gridDim.x * blockDim.x, sh);
 }
 
 __global__ void __launch_bounds__(1024) k_scan_tiles(TiledArgs A) {

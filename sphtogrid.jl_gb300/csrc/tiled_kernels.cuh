@@ -14,10 +14,69 @@
 namespace sphg {
 namespace tiled_detail {
 
+// Maps with at most this many tiles count a CTA's (particle, tile) overlaps
+// in shared memory first, then add them to the global counts once per tile
+// touched (a dense map of few tiles otherwise serialises its particles on
+// a few global counters).
+constexpr int kTileHist = 4096;
+
+// m 2^e as a double, for m a float in [2^-6, 2] and |e| < 1000 (the
+// exponent field of (double)m raised by e; no FP64 arithmetic).
+__device__ __forceinline__ double scale_to_double(float m, int e) {
+  return __longlong_as_double(__double_as_longlong((double)m) + ((long long)e << 52));
+}
+
+// The record's weight factor numerator (w m L^3 / rho, times L in 3D) and
+// 3D mass factor (rho / L^3 * sigma / h^kdim) to FP32 accuracy over the
+// whole FP64 range: FP32 products of the inputs' mantissas, their binary
+// exponents summed as integers.  False (the caller takes FP64) for a zero,
+// subnormal or non-finite input.
+template <int DIMS>
+__device__ __forceinline__ bool factors_f32(const DevMapParams& mp, const PrepLite& q, double* cp, double* aux) {
+  if (!q.f32 || !mp.fac_ok) return false;
+  float wm, mm, rm, hm;
+  int we, me, re, he;
+  split_f(q.w32, wm, we);
+  split_f(q.m32, mm, me);
+  split_f(q.rho32, rm, re);
+  split_f(q.g[3], hm, he);
+  const auto normal = [](float m) { return m >= 0.5f && m < 1.0f; };  // split_f leaves others as they are
+  if (!(normal(fabsf(wm)) && normal(fabsf(mm)) && normal(fabsf(rm)) && normal(fabsf(hm)))) return false;
+  const float Lm = mp.fac_m[0], L3m = mp.fac_m[1], sm = mp.fac_m[2];
+  const int Le = mp.fac_e[0], L3e = mp.fac_e[1], se = mp.fac_e[2];
+  float c = (wm * mm) * L3m / rm;  // [2^-3, 2]
+  int ce = we + me + L3e - re;
+  if (DIMS == 3) {
+    c *= Lm;
+    ce += Le;
+  }
+  const float hk = mp.kernel_dim == 2 ? hm * hm : hm * hm * hm;
+  const float a = (rm * sm) / (hk * L3m);  // [2^-2, 2^4], scaled by 2^-4 below
+  const int ae = re + se - (mp.kernel_dim == 2 ? 2 : 3) * he - L3e + 4;
+  if (!(abs(ce) < 1000 && abs(ae) < 1000)) return false;
+  *cp = scale_to_double(c, ce);
+  *aux = scale_to_double(a * 0.0625f, ae);
+  return true;
+}
+
 // K1 body: this CTA's threads take particles base0 + threadIdx.x, then
 // every `stride` further (a whole CTA enters each iteration together).
+struct PrepShared {
+  int hist[kTileHist];  // overlaps per tile (maps of few tiles)
+  int list[kTileHist];  // tiles touched by this CTA, once each
+  int nlist;
+};
+
 template <int DIMS>
-__device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
+__device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, PrepShared& sh) {
+  int* const s_hist = sh.hist;
+  int* const s_list = sh.list;
+  const bool hist = A.n_tiles <= kTileHist;  // uniform across the CTA
+  if (hist) {
+    for (int i = threadIdx.x; i < (int)A.n_tiles; i += blockDim.x) s_hist[i] = 0;
+    if (threadIdx.x == 0) sh.nlist = 0;
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31;
   unsigned long long c_mapped = 0, c_dep = 0;
   double c_pm = 0.0;
@@ -57,12 +116,17 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
       // rho_pix = rho / L^3; FP32 accuracy suffices here (the FP32 method
       // derives FP32 factors from it; ill-conditioned records redo it in
       // FP64), so no FP64 division
-      const double L = A.mp.L, L3 = L * L * L;
-      const double wm_rho = q.wgt * q.m_in * L3 * rcp_approx(q.rho_in);
-      A.cp[r] = DIMS == 2 ? wm_rho : wm_rho * L;
-      // 3D mass diagnostic factor rho/L^3 * kernel normalisation
-      const double hi_ = rcp_approx(q.hsml);
-      A.aux[r] = q.rho_in * (A.mp.sigma * (A.mp.kernel_dim == 2 ? hi_ * hi_ : hi_ * hi_ * hi_)) * rcp_approx(L3);
+      double cpv, auxv;
+      if (!factors_f32<DIMS>(A.mp, q, &cpv, &auxv)) {
+        const double L = A.mp.L, L3 = L * L * L;
+        const double wm_rho = q.wgt * q.m_in * L3 * rcp_approx(q.rho_in);
+        cpv = DIMS == 2 ? wm_rho : wm_rho * L;
+        // 3D mass diagnostic factor rho/L^3 * kernel normalisation
+        const double hi_ = rcp_approx(q.hsml);
+        auxv = q.rho_in * (A.mp.sigma * (A.mp.kernel_dim == 2 ? hi_ * hi_ : hi_ * hi_ * hi_)) * rcp_approx(L3);
+      }
+      A.cp[r] = cpv;
+      A.aux[r] = auxv;
       for (int k = 0; k < A.pt.nq; ++k)
         A.qv[(int64_t)k * A.cap + r] = q.scalar_zero ? 0.0f
             : A.pt.attr_dtype == 0 ? __ldg((const float*)A.pt.q + p * A.pt.qsp + k * A.pt.qsk)
@@ -74,9 +138,16 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride) {
       const int tz0 = k0 / A.tdim[2], tz1 = (k0 + nk - 1) / A.tdim[2];
       for (int tx = tx0; tx <= tx1; ++tx)
         for (int ty = ty0; ty <= ty1; ++ty)
-          for (int tz = tz0; tz <= tz1; ++tz)
-            atomicAdd(&A.tile_count[((int64_t)tx * A.ntile[1] + ty) * A.ntile[2] + tz], 1);
+          for (int tz = tz0; tz <= tz1; ++tz) {
+            const int64_t t = ((int64_t)tx * A.ntile[1] + ty) * A.ntile[2] + tz;
+            if (!hist) atomicAdd(&A.tile_count[t], 1);
+            else if (atomicAdd(&s_hist[t], 1) == 0) s_list[atomicAdd(&sh.nlist, 1)] = (int)t;
+          }
     }
+  }
+  if (hist) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < sh.nlist; i += blockDim.x) atomicAdd(&A.tile_count[s_list[i]], s_hist[s_list[i]]);
   }
   c_pm = warp_sum_d(c_pm);
   c_mapped = (unsigned long long)warp_sum_ll((long long)c_mapped);
