@@ -61,9 +61,14 @@ constexpr int kTile3X = 8, kTile3Y = 8, kTile3Z = 8;
 //   w[3]  {q0, q1, q2, q3}: the quantities (more than four channels: the
 //         record index in w[3].x, the deposit reads them by record)
 // pack: tile-local index of the box start (10 bits), the box sides minus one
-// (5 bits each, x y z) and the FP64 flag.
+// (5 bits each, x y z), the FP64 flag and the X64 flag.  An FP64 pair with
+// the X64 flag carries its particle's FP64 preparation in place of w[0] and
+// w[3]: w[0] = {x, y} and w[3] = {hsml, 1/hsml} (2D) or {z, hsml} (3D), the
+// pixel coordinates and smoothing length as doubles, so the deposit does
+// not prepare the particle again.
 constexpr int kPairRecWords = 4;  // uint4 per pair record
 constexpr int kPackFP64 = 1 << 25;
+constexpr int kPackX64 = 1 << 26;
 constexpr size_t kPairRecBytes = kPairRecWords * 16;
 
 // Counter ints of one map: tile_count, tile_fill and tile_fill64 per tile,

@@ -447,7 +447,7 @@ __device__ __forceinline__ void finish_scalar(const TiledArgs& A, int64_t r, flo
 // as in the plain path, including its fallback when no centre is inside
 // (cic_2D.jl:196-205, cic_3D.jl:175-184).
 template <int DIMS, int KERN>
-__device__ void finish_fp64_warp(const TiledArgs& A, int64_t r, int lane, double& c_gm, int* emax) {
+__device__ void finish_fp64_warp(const TiledArgs& A, int64_t r, int lane, double& c_gm, int* emax, double* x64) {
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
   const int njk = dm.y * dm.z;
@@ -488,6 +488,11 @@ __device__ void finish_fp64_warp(const TiledArgs& A, int64_t r, int lane, double
     store_factor(A, r, cpv, fabs(cpv) * (fallback ? 1.0 : q.knorm), kRecFP64 | (fallback ? kRecFallback : 0),
                  emax);
   }
+  // the FP64 preparation the record's pairs carry (every lane holds it)
+  x64[0] = q.x;
+  x64[1] = q.y;
+  x64[2] = DIMS == 2 ? q.hsml : q.z;
+  x64[3] = DIMS == 2 ? q.h_inv : q.hsml;
 }
 
 // Tile-range of record r.
@@ -585,7 +590,17 @@ struct PairSrc {
   float tot;        // FP32 record: |numerator| * 2^-cpe
   uint4 q;          // quantities 0-3 (more channels: the record index in q.x)
   bool tight;       // FP32 record: only tiles and cells the support can reach
+  bool x64;         // FP64 record: g and q hold its FP64 preparation (kPackX64)
 };
+
+// An FP64 record's source with its FP64 preparation in place of g and q.
+__device__ __forceinline__ void set_x64(PairSrc& s, const double* v) {
+  s.x64 = true;
+  s.g = make_float4(__int_as_float(__double2loint(v[0])), __int_as_float(__double2hiint(v[0])),
+                    __int_as_float(__double2loint(v[1])), __int_as_float(__double2hiint(v[1])));
+  s.q = make_uint4((unsigned)__double2loint(v[2]), (unsigned)__double2hiint(v[2]), (unsigned)__double2loint(v[3]),
+                   (unsigned)__double2hiint(v[3]));
+}
 
 // The source of record r's pair records, by the lane that finished it
 // (cm, ce: its FP32 factor; FP64 records read their own from memory).
@@ -596,6 +611,7 @@ __device__ __forceinline__ PairSrc pair_src(const TiledArgs& A, int64_t r, bool 
   s.g = A.geo[r];
   s.hinv = 1.0f / s.g.w;
   s.tight = tight;
+  s.x64 = false;
   s.cpm = cm;
   s.cpe = tight ? ce : (int)r;
   // |numerator| relative to 2^cpe (|cpm| S: within the FP32 range for every
@@ -628,7 +644,8 @@ __device__ __forceinline__ void write_pair(const TiledArgs& A, const TileSpan& s
   const int lbase = ((src.bx.x + k0[0] - ox) * A.tdim[1] + (src.bx.y + k0[1] - oy)) * A.tdim[2] +
                     (src.bx.z + k0[2] - oz);
   const unsigned pack = (unsigned)lbase | (unsigned)(k1[0] - k0[0] - 1) << 10 | (unsigned)(k1[1] - k0[1] - 1) << 15 |
-                        (unsigned)(k1[2] - k0[2] - 1) << 20 | (src.tight ? 0u : (unsigned)kPackFP64);
+                        (unsigned)(k1[2] - k0[2] - 1) << 20 | (src.tight ? 0u : (unsigned)kPackFP64) |
+                        (src.x64 ? (unsigned)kPackX64 : 0u);
   const long long slot = src.tight ? A.tile_start[tile] + atomicAdd(&A.tile_fill[tile], 1)
                                    : A.tile_start[tile + 1] - 1 - atomicAdd(&A.tile_fill64[tile], 1);
   uint4* w = A.prec + slot * kPairRecWords;
@@ -651,7 +668,7 @@ __device__ __forceinline__ void flush_stats(const TiledArgs& A, int lane, int di
 }
 
 __device__ __forceinline__ void src_store(uint4* d, const PairSrc& s) {
-  d[0] = make_uint4((unsigned)s.bx.x, (unsigned)s.bx.y, (unsigned)s.bx.z, s.tight ? 1u : 0u);
+  d[0] = make_uint4((unsigned)s.bx.x, (unsigned)s.bx.y, (unsigned)s.bx.z, (s.tight ? 1u : 0u) | (s.x64 ? 2u : 0u));
   d[1] = make_uint4((unsigned)s.dm.x, (unsigned)s.dm.y, (unsigned)s.dm.z, (unsigned)s.dm.w);
   d[2] = make_uint4(__float_as_uint(s.g.x), __float_as_uint(s.g.y), __float_as_uint(s.g.z), __float_as_uint(s.g.w));
   d[3] = make_uint4(__float_as_uint(s.hinv), __float_as_uint(s.cpm), (unsigned)s.cpe, __float_as_uint(s.tot));
@@ -661,7 +678,8 @@ __device__ __forceinline__ PairSrc src_load(const uint4* d) {
   PairSrc s;
   const uint4 a = d[0], b = d[1], g = d[2], f = d[3];
   s.bx = make_int4((int)a.x, (int)a.y, (int)a.z, 0);
-  s.tight = a.w != 0;
+  s.tight = (a.w & 1u) != 0;
+  s.x64 = (a.w & 2u) != 0;
   s.dm = make_int4((int)b.x, (int)b.y, (int)b.z, (int)b.w);
   s.g = make_float4(__uint_as_float(g.x), __uint_as_float(g.y), __uint_as_float(g.z), __uint_as_float(g.w));
   s.hinv = __uint_as_float(f.x);
@@ -758,8 +776,14 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
     }
     const int64_t r = g0 + lane;
     const bool ill = mine && ill_conditioned(my_s, my_u);
-    for (unsigned m = __ballot_sync(0xffffffffu, ill); m; m &= m - 1)
-      finish_fp64_warp<DIMS, KERN>(A, g0 + __ffs(m) - 1, lane, c_gm, emax);
+    double my64[4] = {0.0, 0.0, 0.0, 0.0};
+    for (unsigned m = __ballot_sync(0xffffffffu, ill); m; m &= m - 1) {
+      const int j = __ffs(m) - 1;
+      double v[4];
+      finish_fp64_warp<DIMS, KERN>(A, g0 + j, lane, c_gm, emax, v);
+      if (lane == j)
+        for (int k = 0; k < 4; ++k) my64[k] = v[k];
+    }
     float cm = 0.0f;
     int ce = 0;
     if (mine && !ill) finish_scalar(A, r, my_s, my_c, c_gm, emax, &cm, &ce);
@@ -767,7 +791,8 @@ __device__ void norm_records(const TiledArgs& A, int64_t wid, int64_t nw, int la
     if (!overflow) {
       int4 bx = make_int4(0, 0, 0, 0), dm = bx;
       if (mine) {
-        const PairSrc src = pair_src(A, r, !ill, cm, ce);
+        PairSrc src = pair_src(A, r, !ill, cm, ce);
+        if (ill) set_x64(src, my64);
         bx = src.bx;
         dm = src.dm;
         src_store(srcs[lane], src);
@@ -861,11 +886,14 @@ __device__ void large_finish(const TiledArgs& A, int64_t wid, int64_t nw, int la
         umin = fminf(umin, pv.z);
       }
       warp_reduce_comp(s, comp, umin);
-      if (ill_conditioned(s, umin)) finish_fp64_warp<DIMS, KERN>(A, r, lane, c_gm, emax);
+      const bool ill = ill_conditioned(s, umin);
+      double v[4];
+      if (ill) finish_fp64_warp<DIMS, KERN>(A, r, lane, c_gm, emax, v);
       else if (lane == 0) finish_scalar(A, r, s, comp, c_gm, emax);
       __syncwarp();  // lane 0 wrote the factor
       const bool tight = (A.box[r].w & kRecFP64) == 0;
-      const PairSrc src = pair_src(A, r, tight, A.cpm[r], A.cpe[r]);
+      PairSrc src = pair_src(A, r, tight, A.cpm[r], A.cpe[r]);
+      if (ill) set_x64(src, v);
       const TileSpan sp = tile_span(A, src.bx, src.dm);
       for (int t = lane; t < sp.nt; t += 32) write_pair<DIMS>(A, sp, t, src);
     }
@@ -929,9 +957,10 @@ __device__ __forceinline__ double cell_value(const float* hi, const float* lo, c
 // arithmetic over the pair's whole cell box, lane-strided.  Out of line: its
 // FP64 state stays out of the register budget of the FP32 pair loop.
 template <int DIMS, int KERN, int TY, int TZ, bool DET>
-__device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4 m, const uint4 o, int nq, int TV,
+__device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4* R, int nq, int TV,
                                                float* hi, float* lo, unsigned long long* fx, const double* s_scale,
                                                int lane) {
+  const uint4 m = R[1], o = R[2];
   const int r = (int)m.z;
   const unsigned pack = m.w;
   const int na = (int)((pack >> 10) & 31u) + 1, nb = (int)((pack >> 15) & 31u) + 1, nc = (int)((pack >> 20) & 31u) + 1;
@@ -940,7 +969,21 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4 m
   const int4 bx = A.box[r];
   const int4 dm = A.dimv[r];
   PrepFP64 q;
-  prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
+  if (pack & (unsigned)kPackX64) {
+    // the renormalisation pass's FP64 preparation; 1/hsml and the kernel
+    // normalisation as prep_particle_fp64 forms them
+    const uint4 g = R[0], q4 = R[3];
+    q.x = __hiloint2double((int)g.y, (int)g.x);
+    q.y = __hiloint2double((int)g.w, (int)g.z);
+    const double a = __hiloint2double((int)q4.y, (int)q4.x), b = __hiloint2double((int)q4.w, (int)q4.z);
+    q.z = DIMS == 2 ? 0.0 : a;
+    q.hsml = DIMS == 2 ? a : b;
+    q.h_inv = DIMS == 2 ? b : 1.0 / q.hsml;
+    const double hd = A.mp_re.kernel_dim == 2 ? q.h_inv * q.h_inv : q.h_inv * q.h_inv * q.h_inv;
+    q.knorm = A.mp_re.sigma * hd;
+  } else {
+    prep_bcast<DIMS>(A.pt, A.mp_re, dm.w, lane, &q);
+  }
   const bool fb = (bx.w & kRecFallback) != 0;
   const double cpv = A.cp[r];
   const double scw = s_scale[nq];
@@ -1425,7 +1468,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // FP64 pairs (ill-conditioned records), warp per pair
   for (int j = d0 + warp; j < d1; j += nwarp) {
     const uint4* R = rec64 + (int64_t)j * kPairRecWords;
-    deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, R[1], R[2], nq, TV, hi, lo, fx, s_scale, lane);
+    deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, R, nq, TV, hi, lo, fx, s_scale, lane);
     __syncwarp();
   }
   __syncthreads();
