@@ -294,10 +294,15 @@ __device__ __forceinline__ int prep_particle_fp64(const DevParticles& pt, const 
 struct PrepLite {
   int64_t lo[3], hi[3];     // pix_index_min_max per axis, as PrepFP64
   float g[4];               // x - lo[0], y - lo[1], z - lo[2] and hsml, pixel units
-  double m_in, rho_in, wgt, hsml;
-  float m32, rho32, w32;    // the same as read (f32 set: Float32 inputs)
+  double m_in, rho_in, wgt, hsml;  // set when !f32
+  float m32, rho32, w32;    // set when f32 (Float32 inputs, FP32 preparation)
   bool f32;
   bool scalar_zero;
+
+  __device__ double mass() const { return f32 ? (double)m32 : m_in; }
+  __device__ double rho() const { return f32 ? (double)rho32 : rho_in; }
+  __device__ double weight() const { return f32 ? (double)w32 : wgt; }
+  __device__ double h() const { return f32 ? (double)g[3] : hsml; }
 };
 
 // Error-free a + b == s + e (Knuth's TwoSum; no FMA contraction here).
@@ -320,7 +325,7 @@ __device__ __forceinline__ bool floor_lite(float xh, float xl, float hh, float h
   const float k = floorf(r);
   const float fr = r - k;
   if (!(fr >= delta && fr <= 1.0f - delta)) return false;
-  *out = (int64_t)(a + k);
+  *out = (int)(a + k);  // |a + k| < 2^23: a 32-bit conversion (64-bit ones take the FP64 pipe)
   return true;
 }
 
@@ -330,6 +335,7 @@ __device__ __forceinline__ bool floor_lite(float xh, float xl, float hh, float h
 template <int DIMS>
 __device__ __noinline__ int prep_lite_fp64(const DevParticles& pt, const DevMapParams& mp, int64_t p,
                                            bool store_pos, PrepLite* o) {
+  o->f32 = false;
   PrepFP64 q;
   const int state = prep_particle_fp64<DIMS, false>(pt, mp, p, store_pos, &q);
   if (state == kPrepMapped) {
@@ -450,16 +456,10 @@ __device__ __forceinline__ int prep_particle_lite(const DevParticles& pt, const 
           o->hi[d] = b < P - 1 ? b : P - 1;
           if (o->hi[d] < o->lo[d]) o->hi[d] = o->lo[d] - 1;
           float g1, g2;
-          prep_two_sum(xh, -(float)o->lo[d], g1, g2);
+          prep_two_sum(xh, -(float)(int)o->lo[d], g1, g2);
           o->g[d] = g1 + (g2 + xl);
         }
-        if (!fp64) {
-          o->m_in = (double)o->m32;
-          o->rho_in = (double)o->rho32;
-          o->wgt = (double)o->w32;
-          o->hsml = (double)o->g[3];
-          o->f32 = true;
-        }
+        if (!fp64) o->f32 = true;  // m_in, rho_in, wgt and hsml left to the caller (m32, rho32, w32, g[3])
       }
     }
     if (!fp64) {

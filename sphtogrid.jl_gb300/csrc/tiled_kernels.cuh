@@ -94,7 +94,7 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, Pr
       nk = (int)(q.hi[2] - q.lo[2] + 1);
       c_mapped += 1;
       c_dep += (unsigned long long)ni * nj * nk;
-      c_pm += q.m_in;
+      c_pm += q.mass();
     }
     const bool rec = state == kPrepMapped && ni > 0 && nj > 0 && nk > 0;
     // warp-aggregated slot allocation
@@ -119,11 +119,11 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, Pr
       double cpv, auxv;
       if (!factors_f32<DIMS>(A.mp, q, &cpv, &auxv)) {
         const double L = A.mp.L, L3 = L * L * L;
-        const double wm_rho = q.wgt * q.m_in * L3 * rcp_approx(q.rho_in);
+        const double wm_rho = q.weight() * q.mass() * L3 * rcp_approx(q.rho());
         cpv = DIMS == 2 ? wm_rho : wm_rho * L;
         // 3D mass diagnostic factor rho/L^3 * kernel normalisation
-        const double hi_ = rcp_approx(q.hsml);
-        auxv = q.rho_in * (A.mp.sigma * (A.mp.kernel_dim == 2 ? hi_ * hi_ : hi_ * hi_ * hi_)) * rcp_approx(L3);
+        const double hi_ = rcp_approx(q.h());
+        auxv = q.rho() * (A.mp.sigma * (A.mp.kernel_dim == 2 ? hi_ * hi_ : hi_ * hi_ * hi_)) * rcp_approx(L3);
       }
       A.cp[r] = cpv;
       A.aux[r] = auxv;
