@@ -324,9 +324,8 @@ int sphg_footprints(sphg_context *ctx, const sphg_params *par, const sphg_option
  *   SPHG_ERR_ALLOC leaves the positions as they were, so a retry with the
  *   same options (through sphg_map) centres them once.
  * - The first call on a device looks up the array's device address
- *   (cudaGetSymbolAddress) and keeps it for the process; make that first
- *   call before any stream capture.  The kept address is not valid after a
- *   cudaDeviceReset of that device.
+ *   (cudaGetSymbolAddress) and keeps it for the process.  The kept address
+ *   is not valid after a cudaDeviceReset of that device.
  * - Every call on a device shares the one array and clears what it
  *   accumulates into; calls that overlap on the GPU (other streams or host
  *   threads without ordering between them) race and corrupt each other.
