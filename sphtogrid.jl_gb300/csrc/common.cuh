@@ -357,8 +357,9 @@ __device__ __noinline__ int prep_lite_fp64(const DevParticles& pt, const DevMapP
 }
 
 // The centring, filter, quantity skip and pixel ranges of prep_particle_fp64
-// for FP32 inputs, with the FP64 pipe used only for the centring: the same
-// state, the same centred positions and the same integer ranges, bit for bit.
+// for FP32 inputs, in FP32 arithmetic (FP64 only to centre on a point that
+// is not a float, and for periodic wrapping): the same state, the same
+// centred positions and the same integer ranges, bit for bit.
 //  - The filter compares the centred float against the box rounded inwards
 //    to floats (set_lite_params), which is exact.
 //  - pix_index_min_max takes floor(x -+ h) with x = c L + P/2 and h = hsml L
