@@ -281,6 +281,12 @@ int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);
  * instead of a hang.  Synchronous; allocates a few bytes of device memory. */
 int sphg_probe_wait_timeout(sphg_context *ctx, int32_t polls, int32_t *timed_out);
 
+/* Diagnostics only (no counterpart in the reference): the deterministic
+ * mode's rounding of n host floats v (|v| < 2^62) to integers as three
+ * 21-bit chunks, recombined into x[2 i], beside the 64-bit conversion
+ * (round to nearest, ties to even) in x[2 i + 1].  Synchronous. */
+int sphg_probe_fixed_chunks(sphg_context *ctx, int32_t n, const float *v, int64_t *x);
+
 /* Per-particle state and integer pixel ranges, from the device code every
  * map runs (center_particles and filter_particles_in_image,
  * filter_shift.jl:6-58; the quantity skip, cic_2D.jl:154-168;

@@ -193,6 +193,8 @@ def lib():
         L.sphg_probe_smem_rate.restype = i32
         L.sphg_probe_wait_timeout.argtypes = [vp, i32, C.POINTER(i32)]
         L.sphg_probe_wait_timeout.restype = i32
+        L.sphg_probe_fixed_chunks.argtypes = [vp, i32, vp, vp]
+        L.sphg_probe_fixed_chunks.restype = i32
         L.sphg_accumulate.argtypes = [vp, i64, vp, vp, vp]
         L.sphg_accumulate.restype = i32
         L.sphg_footprints.argtypes = [vp, C.POINTER(SphgParams), C.POINTER(SphgOptions),

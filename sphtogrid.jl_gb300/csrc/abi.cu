@@ -811,6 +811,15 @@ int sphg_healpix_map(sphg_context* ctx, const sphg_healpix_params* hp, int64_t n
   return SPHG_OK;
 }
 
+int sphg_probe_fixed_chunks(sphg_context* ctx, int32_t n, const float* v, int64_t* x) {
+  if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 1 || n > (1 << 24) || !v || !x) return fail(ctx, SPHG_ERR_ARG, "n must be in 1..2^24, arrays non-NULL");
+  DeviceGuard g(ctx->device);
+  CK(sphg::probe_fixed_chunks(n, v, (long long*)x, ctx->stream));
+  return SPHG_OK;
+}
+
 int sphg_probe_wait_timeout(sphg_context* ctx, int32_t polls, int32_t* timed_out) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
   std::lock_guard<std::mutex> lk(ctx->mu);

@@ -338,7 +338,7 @@ int build_plan(sphg_batch* b) {
     o.acc = M.split > 1 ? take((size_t)PD * (nq + 1) * sizeof(double) + M.n_tiles * sizeof(int)) : 0;
     const size_t tv = M.desc.opt.dimensions == 2 ? (size_t)p.tile_x * p.tile_y
                                                  : (size_t)kTile3X * kTile3Y * kTile3Z;
-    smem = std::max(smem, 2 * (size_t)(nq + 1) * tv * sizeof(float));
+    smem = std::max(smem, (p.det ? 3 : 2) * (size_t)(nq + 1) * tv * sizeof(float));
   }
   cudaError_t e = cudaMalloc(&p.mem, off);
   if (e != cudaSuccess) {

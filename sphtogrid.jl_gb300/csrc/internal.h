@@ -30,6 +30,7 @@ void launch_healpix(int64_t nside, int kernel, int kdim, int calc_mean, int dtyp
 constexpr int kHpCtasPerSm = 16;
 cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_per_s);
 cudaError_t probe_wait_timeout(int polls, cudaStream_t s, int* timed_out);
+cudaError_t probe_fixed_chunks(int n, const float* v, long long* x, cudaStream_t s);
 void launch_accumulate(const double* part, double* sum, int64_t len, int num_sms, cudaStream_t s);
 void launch_reduce_3d(const double* q, const double* w, int64_t PD, int w_is_one, double* out,
                       int num_sms, cudaStream_t s);

@@ -83,7 +83,35 @@ __global__ void __launch_bounds__(32) k_probe_wait(int polls, int* timed_out) {
   if (threadIdx.x == 0) *timed_out = done ? 0 : 1;
 }
 
+// The deterministic mode's three-chunk rounding of each v, recombined, next
+// to the 64-bit conversion it must equal.
+__global__ void __launch_bounds__(256) k_probe_chunks(const float* v, long long* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int x0, x1, x2;
+  tiled_detail::fixed_chunks(v[i], x0, x1, x2);
+  out[2 * i] = (long long)x2 * (1LL << 42) + (long long)x1 * (1LL << 21) + x0;
+  out[2 * i + 1] = __float2ll_rn(v[i]);
+}
+
 }  // namespace
+
+cudaError_t probe_fixed_chunks(int n, const float* v, long long* x, cudaStream_t s) {
+  float* dv = nullptr;
+  long long* dx = nullptr;
+  cudaError_t e = cudaMalloc(&dv, (size_t)n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dx, 2 * (size_t)n * sizeof(long long));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_probe_chunks<<<(n + 255) / 256, 256, 0, s>>>(dv, dx, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(x, dx, 2 * (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (dv) cudaFree(dv);
+  if (dx) cudaFree(dx);
+  return e;
+}
 
 cudaError_t probe_wait_timeout(int polls, cudaStream_t s, int* timed_out) {
   int* d = nullptr;

@@ -917,34 +917,70 @@ __device__ __forceinline__ long long float_to_ll_split(float v) {
   return (long long)h * 2147483648LL + (long long)__float2int_rz(fmaf(-(float)h, 0x1p31f, v));
 }
 
+// Tiles (or chunks of split tiles) of at most this many pairs accumulate the
+// deterministic mode's fixed point as three 21-bit chunks: a cell takes at
+// most one value per pair, each chunk of a value is at most 2^20 in
+// magnitude, so no 32-bit chunk sum can overflow.
+constexpr int kChunkPairs = 2047;
+
+// v (|v| < 2^62) rounded to the nearest integer x = x2 2^42 + x1 2^21 + x0,
+// |xk| <= 2^20, by FP32 additions alone: a float of magnitude below
+// 2^(22+k) added to 1.5 2^(23+k) leaves round(v / 2^k) in the sum's low
+// mantissa bits (its ulp is 2^k), and each remainder is exact.  The sum of
+// the three parts is round(v) with ties to even, as a 64-bit conversion
+// rounds, since x2 2^42 + x1 2^21 is even.
+__device__ __forceinline__ void fixed_chunks(float v, int& x0, int& x1, int& x2) {
+  const float C42 = 0x1.8p65f, C21 = 0x1.8p44f, C0 = 0x1.8p23f;
+  const float t2 = v + C42;
+  const float r1 = v - (t2 - C42);
+  const float t1 = r1 + C21;
+  const float r0 = r1 - (t1 - C21);
+  const float t0 = r0 + C0;
+  x2 = __float_as_int(t2) - __float_as_int(C42);
+  x1 = __float_as_int(t1) - __float_as_int(C21);
+  x0 = __float_as_int(t0) - __float_as_int(C0);
+}
+
 // Adds one cell value to a tile accumulator (see k_deposit).  DET: an exact
-// int64 fixed-point sum held as two 32-bit words, the low words in the first
-// plane (`hi`), the high words in the second (`lo`).  Shared-memory atomics on
-// 32-bit integers are single native instructions, while 64-bit and FP32 ones
-// are compiled to load / compare-and-swap loops; the low word's add returns
-// its old value, from which the carry into the high word follows, so the
-// pair adds exactly modulo 2^64 whatever the order of the additions.
+// int64 fixed-point sum.  Shared-memory atomics on 32-bit integers are single
+// native instructions, while 64-bit and FP32 ones are compiled to load /
+// compare-and-swap loops.  With c2 (a tile of at most kChunkPairs pairs) the
+// value's three chunks go into the planes hi, lo and c2 as signed 32-bit
+// sums, three reductions that return nothing; otherwise the low and high
+// words go into hi and lo, the low word's add returning its old value, from
+// which the carry into the high word follows.  Both add exactly whatever the
+// order of the additions.
 template <bool DET, bool SPLIT = false>
-__device__ __forceinline__ void acc_cell(float* hi, float* lo, unsigned long long* fx, int i, float v) {
+__device__ __forceinline__ void acc_cell(float* hi, float* lo, int* c2, int i, float v) {
   if (DET) {
-    const unsigned long long x = (unsigned long long)(SPLIT ? float_to_ll_split(v) : __float2ll_rn(v));
-    const unsigned xl = (unsigned)x;
-    const unsigned old = atomicAdd((unsigned*)hi + i, xl);
-    const unsigned xh = (unsigned)(x >> 32) + (old + xl < old ? 1u : 0u);
-    if (xh != 0u) atomicAdd((unsigned*)lo + i, xh);
+    if (c2) {
+      int x0, x1, x2;
+      fixed_chunks(v, x0, x1, x2);
+      atomicAdd((int*)hi + i, x0);
+      atomicAdd((int*)lo + i, x1);
+      atomicAdd(c2 + i, x2);
+    } else {
+      const unsigned long long x = (unsigned long long)(SPLIT ? float_to_ll_split(v) : __float2ll_rn(v));
+      const unsigned xl = (unsigned)x;
+      const unsigned old = atomicAdd((unsigned*)hi + i, xl);
+      const unsigned xh = (unsigned)(x >> 32) + (old + xl < old ? 1u : 0u);
+      if (xh != 0u) atomicAdd((unsigned*)lo + i, xh);
+    }
   } else {
     acc_twosum(&hi[i], &lo[i], v);
   }
 }
 
 // The exact int64 value of a DET accumulator cell.
-__device__ __forceinline__ long long fixed_value(const float* hi, const float* lo, int i) {
+__device__ __forceinline__ long long fixed_value(const float* hi, const float* lo, const int* c2, int i) {
+  if (c2)
+    return (long long)c2[i] * (1LL << 42) + (long long)((const int*)lo)[i] * (1LL << 21) + ((const int*)hi)[i];
   return (long long)(((unsigned long long)((const unsigned*)lo)[i] << 32) | ((const unsigned*)hi)[i]);
 }
 
 template <bool DET>
-__device__ __forceinline__ double cell_value(const float* hi, const float* lo, const unsigned long long* fx, int i) {
-  if (DET) return (double)fixed_value(hi, lo, i);
+__device__ __forceinline__ double cell_value(const float* hi, const float* lo, const int* c2, int i) {
+  if (DET) return (double)fixed_value(hi, lo, c2, i);
   return (double)hi[i] + (double)lo[i];
 }
 
@@ -958,7 +994,7 @@ __device__ __forceinline__ double cell_value(const float* hi, const float* lo, c
 // FP64 state stays out of the register budget of the FP32 pair loop.
 template <int DIMS, int KERN, int TY, int TZ, bool DET>
 __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4* R, int nq, int TV,
-                                               float* hi, float* lo, unsigned long long* fx, const double* s_scale,
+                                               float* hi, float* lo, int* c2, const double* s_scale,
                                                int lane) {
   const uint4 m = R[1], o = R[2];
   const int r = (int)m.z;
@@ -999,9 +1035,9 @@ __device__ __noinline__ void deposit_pair_fp64(const TiledArgs& A, const uint4* 
     const double pw = wk * ar * cpv;
     if (pw != 0.0) {
       const int li = lbase + (a * TY + b) * TZ + c;
-      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, __double2float_rn(pw * scw));
+      acc_cell<DET, DIMS == 2>(hi, lo, c2, nq * TV + li, __double2float_rn(pw * scw));
       for (int k = 0; k < nq; ++k)
-        acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li,
+        acc_cell<DET, DIMS == 2>(hi, lo, c2, k * TV + li,
                                  __double2float_rn(pw * s_scale[k] * (double)A.qv[(int64_t)k * A.cap + r]));
     }
   }
@@ -1096,8 +1132,12 @@ __device__ __forceinline__ void store_cell(const TiledArgs& A, int64_t P, int64_
     A.out[row + (int64_t)nq * PD] = W;
     for (int c = 0; c < nq; ++c) A.out[row + c * PD] = q(c);
   } else if (DIMS == 3) {
+    // reduce_image_3D divides wherever Q > 0 (reduce_image.jl:49-51); a
+    // weight sum that vanished in the tile accumulator (below the
+    // deterministic mode's fixed-point quantum, or FP32 underflow) leaves
+    // the cell empty rather than infinite
     double Q = q(0);
-    if (Q > 0.0) Q /= (A.w_is_one ? 1.0 : W);
+    if (Q > 0.0 && !A.w_is_one) Q = W > 0.0 ? Q / W : 0.0;
     A.out[((int64_t)i * P + j) * P + k] = Q;
   } else {
     for (int c = 0; c < nq; ++c) {
@@ -1142,7 +1182,7 @@ __device__ __forceinline__ float channel_factor(float q, float cpm, int cpe, int
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
 __device__ __forceinline__ void deposit_cell(const float2 (*tab)[32], int a, int b, int c, int lbase, float hinv,
                                              float cw, const float* cq, int nq, int TV, float* hi, float* lo,
-                                             unsigned long long* fx) {
+                                             int* c2) {
   // 2D: the z term is the constant {0, 1} (the same u and weight as the
   // renormalisation pass forms)
   {
@@ -1151,11 +1191,11 @@ __device__ __forceinline__ void deposit_cell(const float2 (*tab)[32], int a, int
     if (u <= 1.0f) {
       const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
       const int li = lbase + (a * TY + b) * TZ + c;
-      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, gw * cw);
+      acc_cell<DET, DIMS == 2>(hi, lo, c2, nq * TV + li, gw * cw);
 #pragma unroll
       for (int k = 0; k < (NQ > 0 ? NQ : kMaxQ); ++k) {
         if (NQ == 0 && k >= nq) break;
-        acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li, gw * cq[k]);
+        acc_cell<DET, DIMS == 2>(hi, lo, c2, k * TV + li, gw * cq[k]);
       }
     }
   }
@@ -1167,14 +1207,14 @@ __device__ __forceinline__ void deposit_cell(const float2 (*tab)[32], int a, int
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
 __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, int nb, int nc, int lbase, float hinv,
                                               float cw, const float* cq, int nq, int TV, float* hi, float* lo,
-                                              unsigned long long* fx, int lane) {
+                                              int* c2, int lane) {
   const float inv_nc = inv_small(nc), inv_nb = inv_small(nb);
   for (int e = lane; e < n; e += 32) {
     const int bc = DIMS == 3 ? fdiv(e, inv_nc) : e;  // 2D: nc == 1
     const int cc = DIMS == 3 ? e - bc * nc : 0;
     const int ca = fdiv(bc, inv_nb);
     const int cb = bc - ca * nb;
-    deposit_cell<DIMS, KERN, NQ, TY, TZ, DET>(tab, ca, cb, cc, lbase, hinv, cw, cq, nq, TV, hi, lo, fx);
+    deposit_cell<DIMS, KERN, NQ, TY, TZ, DET>(tab, ca, cb, cc, lbase, hinv, cw, cq, nq, TV, hi, lo, c2);
   }
 }
 
@@ -1182,7 +1222,7 @@ __device__ __forceinline__ void deposit_cells(const float2 (*tab)[32], int n, in
 // cell box, then its cells.  Uniform across the warp.
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
 __device__ __forceinline__ void deposit_pair32(const TiledArgs& A, const uint4* R, int nq, int TV, const int* s_shift,
-                                               float2 (*tab)[32], float* hi, float* lo, unsigned long long* fx,
+                                               float2 (*tab)[32], float* hi, float* lo, int* c2,
                                                int lane) {
   const uint4 g = R[0], m = R[1], o = R[2];
   const unsigned pack = m.w;
@@ -1219,7 +1259,7 @@ __device__ __forceinline__ void deposit_pair32(const TiledArgs& A, const uint4* 
   // a run-time kernel shape is dispatched once per pair, so the cell loop
   // evaluates a compile-time shape
 #define SPHG_CELLS(K) \
-  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, lbase, hinv, cw, cq, nq, TV, hi, lo, fx, lane)
+  deposit_cells<DIMS, K, NQ, TY, TZ, DET>(tab, n, nb, nc, lbase, hinv, cw, cq, nq, TV, hi, lo, c2, lane)
   if (KERN >= 0) SPHG_CELLS(KERN >= 0 ? KERN : 0);
   else if (A.kern == 0) SPHG_CELLS(0);
   else if (A.kern == 1) SPHG_CELLS(1);
@@ -1266,7 +1306,7 @@ __device__ __forceinline__ void small_header(const uint4* R, const int* s_shift,
 // pairs may meet in one step; the accumulation is atomic.
 template <int DIMS, int KERN, int NQ, int TY, int TZ, bool DET>
 __device__ __forceinline__ void deposit_small(const uint4* R, unsigned smask, int nj, const int* s_shift, int nq,
-                                              int TV, uint4 (*hdr)[4], float* hi, float* lo, unsigned long long* fx,
+                                              int TV, uint4 (*hdr)[4], float* hi, float* lo, int* c2,
                                               int lane) {
   const unsigned full = 0xffffffffu;
   const bool mine = (smask >> lane) & 1u;
@@ -1304,11 +1344,11 @@ __device__ __forceinline__ void deposit_small(const uint4* R, unsigned smask, in
     if (u <= 1.0f) {
       const float gw = kshape_f<KERN>(u) * (ex.y * ey.y * ez.y);
       const int li = (int)(h2.y & 1023u) + (a * TY + b) * TZ + c;
-      acc_cell<DET, DIMS == 2>(hi, lo, fx, nq * TV + li, gw * __uint_as_float(h1.y));
+      acc_cell<DET, DIMS == 2>(hi, lo, c2, nq * TV + li, gw * __uint_as_float(h1.y));
       const uint4 q4 = hdr[j][3];
       const float cq[4] = {__uint_as_float(q4.x), __uint_as_float(q4.y), __uint_as_float(q4.z), __uint_as_float(q4.w)};
 #pragma unroll
-      for (int k = 0; k < (NQ > 0 && NQ <= 4 ? NQ : 1); ++k) acc_cell<DET, DIMS == 2>(hi, lo, fx, k * TV + li, gw * cq[k]);
+      for (int k = 0; k < (NQ > 0 && NQ <= 4 ? NQ : 1); ++k) acc_cell<DET, DIMS == 2>(hi, lo, c2, k * TV + li, gw * cq[k]);
     }
   }
   __syncwarp();  // the headers are rewritten for the next chunk
@@ -1320,16 +1360,15 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   constexpr int TV = TX * TY * TZ;
   const int nq = NQ > 0 ? NQ : A.pt.nq;
   const int nch = nq + 1;
-  // FP32C: hi [nch][TV], lo [nch][TV]; DET: low words [nch][TV] in `hi`,
-  // high words [nch][TV] in `lo`
+  // FP32C: hi [nch][TV], lo [nch][TV]; DET: three planes [nch][TV] (see
+  // acc_cell), the third used when the tile has at most kChunkPairs pairs
   float* hi = (float*)smem_raw;
   float* lo = hi + nch * TV;
-  unsigned long long* fx = (unsigned long long*)smem_raw;  // DET: [nch][TV]
   const int tz = (int)(t % A.ntile[2]);
   const int ty = (int)((t / A.ntile[2]) % A.ntile[1]);
   const int tx = (int)(t / ((int64_t)A.ntile[2] * A.ntile[1]));
   const int ox = tx * TX, oy = ty * TY, oz = tz * TZ;
-  for (int v = threadIdx.x; v < 2 * nch * TV; v += blockDim.x) hi[v] = 0.0f;
+  for (int v = threadIdx.x; v < (DET ? 3 : 2) * nch * TV; v += blockDim.x) hi[v] = 0.0f;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   // after an overflow of the pair list the lists are incomplete: deposit
   // nothing (the host grows the list and maps again); nor after a staging
@@ -1348,6 +1387,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   const int f1 = split ? (int)((long long)n32 * (chunk + 1) / A.split) : n32;
   const int d0 = split ? (int)((long long)n64 * chunk / A.split) : 0;
   const int d1 = split ? (int)((long long)n64 * (chunk + 1) / A.split) : n64;
+  int* const c2 = (DET && (f1 - f0) + (d1 - d0) <= kChunkPairs) ? (int*)(lo + nch * TV) : nullptr;
   // channel scales (powers of two): 2^s_shift as double for the flush
   double* s_scale = sh.scale;
   double* s_unscale = sh.unscale;
@@ -1444,7 +1484,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
         smask = __ballot_sync(0xffffffffu, lane < cnt && nj <= kSmallCells);
         if (smask) {
 #define SPHG_SMALL(K) \
-  deposit_small<DIMS, K, NQ, TY, TZ, DET>(R, smask, nj, s_shift, nq, TV, sh.small[warp & 7], hi, lo, fx, lane)
+  deposit_small<DIMS, K, NQ, TY, TZ, DET>(R, smask, nj, s_shift, nq, TV, sh.small[warp & 7], hi, lo, c2, lane)
           if (KERN >= 0) SPHG_SMALL(KERN >= 0 ? KERN : 0);
           else if (A.kern == 0) SPHG_SMALL(0);
           else if (A.kern == 1) SPHG_SMALL(1);
@@ -1456,7 +1496,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       }
       for (int j = 0; j < cnt; ++j)
         if (!((smask >> j) & 1u))
-          deposit_pair32<DIMS, KERN, NQ, TY, TZ, DET>(A, R + j * kPairRecWords, nq, TV, s_shift, tab, hi, lo, fx,
+          deposit_pair32<DIMS, KERN, NQ, TY, TZ, DET>(A, R + j * kPairRecWords, nq, TV, s_shift, tab, hi, lo, c2,
                                                       lane);
       __syncwarp();
       if (lane == 0) fence_proxy_async_smem();  // this buffer's reads before its next bulk copy
@@ -1468,7 +1508,7 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
   // FP64 pairs (ill-conditioned records), warp per pair
   for (int j = d0 + warp; j < d1; j += nwarp) {
     const uint4* R = rec64 + (int64_t)j * kPairRecWords;
-    deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, R, nq, TV, hi, lo, fx, s_scale, lane);
+    deposit_pair_fp64<DIMS, KERN, TY, TZ, DET>(A, R, nq, TV, hi, lo, c2, s_scale, lane);
     __syncwarp();
   }
   __syncthreads();
@@ -1485,10 +1525,10 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
       const int64_t row = DIMS == 2 ? (int64_t)i * P + j : ((int64_t)i * P + j) * P + k;
       for (int c = 0; c <= nq; ++c) {
         if (DET) {
-          const unsigned long long x = (unsigned long long)fixed_value(hi, lo, c * TV + li);
+          const unsigned long long x = (unsigned long long)fixed_value(hi, lo, c2, c * TV + li);
           if (x) atomicAdd((unsigned long long*)A.acc + row + c * PD, x);
         } else {
-          const double x = cell_value<DET>(hi, lo, fx, c * TV + li);
+          const double x = cell_value<DET>(hi, lo, c2, c * TV + li);
           if (x != 0.0) atomicAdd(A.acc + row + c * PD, x * s_unscale[c]);
         }
       }
@@ -1519,9 +1559,9 @@ __device__ void deposit_tile(const TiledArgs& A, int64_t t, unsigned char* smem_
     int li, i, j, k;
     flush_cell<DIMS, TX, TY, TZ>(A, v, ox, oy, oz, DIMS == 2 && A.mode == 0, li, i, j, k);
     if (i >= P || j >= P || (DIMS == 3 && k >= P)) continue;
-    const double W = cell_value<DET>(hi, lo, fx, nq * TV + li) * inv_w;
+    const double W = cell_value<DET>(hi, lo, c2, nq * TV + li) * inv_w;
     store_cell<DIMS>(A, P, PD, i, j, k, nq, W,
-                     [&](int c) { return cell_value<DET>(hi, lo, fx, c * TV + li) * s_unscale[c]; });
+                     [&](int c) { return cell_value<DET>(hi, lo, c2, c * TV + li) * s_unscale[c]; });
   }
   __syncthreads();  // the shared accumulators are reused by the next tile
 }
@@ -1542,13 +1582,13 @@ void launch_deposit_det(const TiledArgs& A, cudaStream_t s) {
   // above the default 48 KB in all the kernel opts in
   if (DIMS == 2) {
     constexpr int TX = 16, TY = 16;
-    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
+    const size_t sm = (DET ? 3 : 2) * (size_t)(A.pt.nq + 1) * TX * TY * sizeof(float);
     if (sm + sizeof(DepositShared) > 48 * 1024)
       cudaFuncSetAttribute(k_deposit<2, KERN, NQ, TX, TY, 1, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_deposit<2, KERN, NQ, TX, TY, 1, DET><<<(unsigned)A.n_tiles, 256, sm, s>>>(A);
   } else {
     constexpr int TX = kTile3X, TY = kTile3Y, TZ = kTile3Z;
-    const size_t sm = 2 * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
+    const size_t sm = (DET ? 3 : 2) * (size_t)(A.pt.nq + 1) * TX * TY * TZ * sizeof(float);
     if (sm + sizeof(DepositShared) > 48 * 1024)
       cudaFuncSetAttribute(k_deposit<3, KERN, NQ, TX, TY, TZ, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)sm);
