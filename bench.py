@@ -806,7 +806,7 @@ def _onchip_ceiling(L, ctx, _lib, value, other, det):
     library's conflict-free microbenchmark, and the fraction reached."""
     names = {0: "fp32_atomic_with_return", 1: "fp32_atomic_no_return", 2: "int64_atomic",
              3: "fp32_compensated_add_two_atomics", 4: "fp32_compensated_pair_cas",
-             5: "int64_fixed_point_two_u32_atomics"}
+             5: "int64_fixed_point_two_u32_atomics", 6: "int64_fixed_point_three_chunk_reductions"}
     rates = {}
     for kind, nm in names.items():
         r = C.c_double()
@@ -814,7 +814,7 @@ def _onchip_ceiling(L, ctx, _lib, value, other, det):
         rates[nm] = r.value
     chans = 2
     ceil_c = rates["fp32_compensated_add_two_atomics"] / chans  # the FP32C deposit's accumulation
-    ceil_d = rates["int64_fixed_point_two_u32_atomics"] / chans  # the deterministic deposit's
+    ceil_d = rates["int64_fixed_point_three_chunk_reductions"] / chans  # the deterministic deposit's (tiles of <= 2047 pairs)
     v_c = value if not det else (other or {}).get("value")
     v_d = value if det else (other or {}).get("value")
     return {"smem_additions_per_s": rates, "channel_additions_per_deposit": chans,

@@ -269,7 +269,9 @@ int sphg_adjoint(sphg_context *ctx, const sphg_params *par, const sphg_options *
  * accumulator); 4: the same compensated add of an adjacent (hi, lo) pair by
  * one 64-bit compare-and-swap (an alternative, not used); 5: the
  * deterministic deposit's int64 fixed-point add as two native 32-bit atomics
- * with a carry.
+ * with a carry (its tiles of more than 2047 pairs); 6: the same fixed point
+ * as three 21-bit chunks added by three 32-bit reductions (its tiles of at
+ * most 2047 pairs).
  * Conflict-free addresses: an upper bound, not a deposit rate.  Synchronous;
  * allocates a few bytes of device memory. */
 int sphg_probe_smem_rate(sphg_context *ctx, int kind, double *ops_per_s);

@@ -834,7 +834,7 @@ int sphg_probe_wait_timeout(sphg_context* ctx, int32_t polls, int32_t* timed_out
 int sphg_probe_smem_rate(sphg_context* ctx, int kind, double* ops_per_s) {
   if (!ctx) return fail(nullptr, SPHG_ERR_ARG, "context is NULL");
   std::lock_guard<std::mutex> lk(ctx->mu);
-  if (!ops_per_s || kind < 0 || kind > 5) return fail(ctx, SPHG_ERR_ARG, "kind must be 0..5");
+  if (!ops_per_s || kind < 0 || kind > 6) return fail(ctx, SPHG_ERR_ARG, "kind must be 0..6");
   DeviceGuard g(ctx->device);
   CK(sphg::probe_smem_rate(kind, ctx->num_sms, ctx->stream, ops_per_s));
   return SPHG_OK;

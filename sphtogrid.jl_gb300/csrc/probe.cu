@@ -11,8 +11,11 @@
 // accumulator, the FP32C deposit's); 4 the same compensated add of an
 // adjacent (hi, lo) pair by one 64-bit compare-and-swap (not used by the
 // deposit); 5 the deterministic deposit's int64 fixed-point add as two native
-// 32-bit atomics with a carry.  Lanes of a warp address distinct banks, as the cells of one
-// deposit iteration do, so the figure is the conflict-free ceiling.
+// 32-bit atomics with a carry (its tiles of more than 2047 pairs); 6 the same
+// fixed point as three 21-bit chunks, three 32-bit reductions without
+// return (its tiles of at most 2047 pairs).  Lanes of a warp address
+// distinct banks, as the cells of one deposit iteration do, so the figure is
+// the conflict-free ceiling.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -49,6 +52,14 @@ __global__ void __launch_bounds__(256, 4) k_probe_smem(float* sink) {
       acc_twosum(&hi[idx], &lo[idx], v);
     } else if (KIND == 4) {
       acc_pair(reinterpret_cast<float2*>(raw) + idx, v);
+    } else if (KIND == 6) {  // three 21-bit chunks (planes of kProbeCells / 2 cells)
+      int* w = reinterpret_cast<int*>(raw);
+      const int j = idx & (kProbeCells / 2 - 1);
+      int x0, x1, x2;
+      tiled_detail::fixed_chunks(v * 1.0e9f, x0, x1, x2);
+      atomicAdd(&w[j], x0);
+      atomicAdd(&w[kProbeCells / 2 + j], x1);
+      atomicAdd(&w[kProbeCells + j], x2);
     } else {  // int64 fixed point as two native 32-bit words with a carry
       unsigned* w = reinterpret_cast<unsigned*>(raw);
       const unsigned long long x = (unsigned long long)(long long)(v * 1.0e9f);
@@ -142,7 +153,8 @@ cudaError_t probe_smem_rate(int kind, int num_sms, cudaStream_t s, double* ops_p
       case 2: launch_probe<2>(grid, sink, s); break;
       case 3: launch_probe<3>(grid, sink, s); break;
       case 4: launch_probe<4>(grid, sink, s); break;
-      default: launch_probe<5>(grid, sink, s); break;
+      case 5: launch_probe<5>(grid, sink, s); break;
+      default: launch_probe<6>(grid, sink, s); break;
     }
     cudaEventRecord(e1, s);
     e = cudaEventSynchronize(e1);
