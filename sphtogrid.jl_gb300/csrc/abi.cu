@@ -885,6 +885,7 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   // FP32C: the image gradients in FP32 too, for the FP32 per-cell path
   const bool f32 = opt->precision == SPHG_PREC_FP32C;
   const size_t o_g32 = f32 ? cv.take((size_t)PD * (nq + 1) * sizeof(float)) : 0;
+  const size_t o_adj = f32 ? cv.take(sphg::adjoint_scratch_bytes(n)) : 0;
   if (int st = ensure_ws(ctx, cv.off, s)) return st;
   double* gq = (double*)((char*)ctx->ws + o_g);
   double* gw = gq + (int64_t)nq * PD;
@@ -922,7 +923,8 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   mp.sigma = sphg::kernel_sigma(opt->kernel, opt->kernel_dim);
   const bool raw_out = opt->raw_accumulator || (dims == 2 && opt->return_both_maps);
   CK(sphg::launch_adjoint(opt->kernel, d, mp, raw, grad_out, raw_out ? 1 : 0, opt->reduce_image, gq, gw,
-                          gr->pos, gr->hsml, gr->mass, gr->rho, gr->weights, gr->bin_q, g32, ctx->num_sms, s));
+                          gr->pos, gr->hsml, gr->mass, gr->rho, gr->weights, gr->bin_q, g32,
+                          f32 ? (char*)ctx->ws + o_adj : nullptr, ctx->num_sms, s));
   if (!stream) CK(cudaStreamSynchronize(s));
   ctx->last_error.clear();
   return SPHG_OK;

@@ -143,6 +143,18 @@ __global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ r
   }
 }
 
+// FP32 path: a particle whose FP32 result misses the relative test of its
+// own values waits for the second pass with its error estimates in output
+// units (pos x, y, z and hsml; the absolute error of dL/dK; q_0..q_3).
+struct AdjPending {
+  long long p;
+  float e[9];
+  float pad;
+};
+// Scales of the second pass's test: the largest |value| of each output kind
+// over all particles (float bits, atomic max): pos, hsml, mass, rho, w, q.
+constexpr int kAdjScales = 6;
+
 struct AdjArgs {
   DevParticles pt;
   DevMapParams mp;
@@ -154,6 +166,9 @@ struct AdjArgs {
   double *d_hsml, *d_mass, *d_rho, *d_w;
   double* d_q;       // strides of pt.q
   DevStatus* st;
+  unsigned* scale;   // FP32 path: [kAdjScales], then the pending count
+  unsigned* n_pend;
+  AdjPending* pend;  // [n]
 };
 
 // Maps of at most this many quantities take the FP32 path.
@@ -303,19 +318,21 @@ constexpr float kTermEps = 5e-7f;
 constexpr float kEdgeEps = 6e-7f;
 constexpr double kKeepRel = 2e-5;
 
-// One mapped particle on the FP32 path; false (nothing written) for the
-// particles it leaves to the FP64 path: those the forward redoes in FP64,
-// and those whose sums cancel so that the FP32 terms' rounding bound exceeds
-// kKeepRel of a result (typically a particle with a near-zero gradient next
-// to pixels of tiny W, where dL/dW is large).
+// One mapped particle on the FP32 path.  Returns 0 (nothing computed) for
+// the particles it leaves to the FP64 path, those the forward redoes in
+// FP64; 1 when every result passes the relative test (its rounding estimate
+// within kKeepRel of it); 2 when some result does not -- typically a
+// near-zero gradient whose terms cancel next to pixels of tiny W, where
+// dL/dW is large -- after lane 0 has queued the particle with its error
+// estimates for the second pass (k_adj_pending).
 template <int DIMS, int KERN>
-__device__ bool adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
-                                  double& dK, double* dqk) {
+__device__ int adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
+                                 double& dK, double* dqk) {
   const DevParticles& pt = A.pt;
   const int nq = pt.nq;
-  if (nq > kAdjQ32) return false;
+  if (nq > kAdjQ32) return 0;
   const int64_t ni = q.hi[0] - q.lo[0] + 1, nj = q.hi[1] - q.lo[1] + 1, nk = q.hi[2] - q.lo[2] + 1;
-  if (ni * nj * nk >= (1 << 20)) return false;
+  if (ni * nj * nk >= (1 << 20)) return 0;
   const int F = (int)(ni * nj * nk), njk = (int)(nj * nk), nkk = (int)nk;
   const float inv_njk = inv_small(njk), inv_nk = inv_small(nkk);
   // the particle relative to its footprint origin (FP64 -> FP32 once)
@@ -359,7 +376,7 @@ __device__ bool adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) umin = fminf(umin, __shfl_xor_sync(0xffffffffu, umin, o));
   const double S1 = comp_total(s1, c1);
-  if (ill_conditioned((float)S1, umin)) return false;  // warp-uniform
+  if (ill_conditioned((float)S1, umin)) return 0;  // warp-uniform
   const float Gam1 = (float)(comp_total(sG1, cG1) / S1);
   // pass 2: g, its derivatives and the image gradients (compensated sums)
   float aS = 0, cS = 0, aG = 0, cG = 0, agd[4] = {}, cgd[4] = {}, ad[4] = {}, cd[4] = {};
@@ -428,70 +445,183 @@ __device__ bool adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q
     Bd[t] = 3.0 * sqrt(wsum((double)bd[t]));
   }
   for (int k = 0; k < kAdjQ32; ++k) Bq[k] = 3.0 * sqrt(wsum((double)bq[k]));
-  if (!(S > 0.0)) return false;
+  if (!(S > 0.0)) return 0;
   const double Gam = sgg / S;
   const double relG = BG / fabs(sgg);  // relative error of Gam (S is a sum of positive terms)
   bool keep = !(relG > kKeepRel);  // (0 / 0 when every term is 0: kept)
   // sum (gam - Gam) dg = sum (gam - Gam1) dg - (Gam - Gam1) sum dg
   const double dG = Gam - (double)Gam1;
-  double val[4];
+  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
+  double val[4], err[4];
   for (int t = 0; t < 4; ++t) {
     val[t] = sgd[t] - dG * sd[t];
-    const double err = Bgd[t] + fabs(dG) * Bd[t] + fabs(Gam * sd[t]) * (sgg != 0.0 ? relG : 0.0);
-    if (err > kKeepRel * fabs(val[t])) keep = false;
+    err[t] = Bgd[t] + fabs(dG) * Bd[t] + fabs(Gam * sd[t]) * (sgg != 0.0 ? relG : 0.0);
+    if (err[t] > kKeepRel * fabs(val[t])) keep = false;
   }
   for (int k = 0; k < nq; ++k)
     if (Bq[k] > kKeepRel * fabs(sq[k])) keep = false;
-  if (!keep) return false;  // warp-uniform: every value is a warp sum
-  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
   dK = Gam;
   for (int t = 0; t < 4; ++t) grad[t] = K / S * val[t];
   for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
-  return true;
+  if (keep) return 1;  // warp-uniform: every value is a warp sum
+  if (lane == 0) {  // errors in output units: pos and hsml carry L, as the outputs do
+    AdjPending e;
+    e.p = p;
+    for (int t = 0; t < 4; ++t) e.e[t] = (float)(fabs(K / S) * err[t] * A.mp.L);
+    e.e[4] = (float)(BG / S);
+    for (int k = 0; k < kAdjQ32; ++k) e.e[5 + k] = k < nq ? (float)(fabs(K / S) * Bq[k]) : 0.0f;
+    e.pad = 0.0f;
+    A.pend[atomicAdd(A.n_pend, 1u)] = e;
+  }
+  return 2;
 }
 
+// Lane 0 writes particle p's derivatives (dK, grad in pixel units, dqk)
+// into the outputs and returns, in v, their magnitudes per output kind.
+template <int DIMS>
+__device__ void write_outputs(const AdjArgs& A, int64_t p, int state, const PrepFP64& q, const double grad[4],
+                              double dK, const double* dqk, float v[kAdjScales]) {
+  const DevParticles& pt = A.pt;
+  const double L = A.mp.L;
+  // K = w m L^3 / rho (2D), times L in 3D
+  const double LD = DIMS == 2 ? L * L * L : L * L * L * L;
+  const double m_in = state == kPrepMapped ? q.m_in : 0.0;
+  const double rho_in = state == kPrepMapped ? q.rho_in : 1.0;
+  const double w_in = state == kPrepMapped ? q.wgt : 0.0;
+  const double dw = dK * m_in * LD / rho_in, dm = dK * w_in * LD / rho_in;
+  const double dr = -dK * w_in * m_in * LD / (rho_in * rho_in);
+  A.d_w[p] = dw;
+  A.d_mass[p] = dm;
+  A.d_rho[p] = dr;
+  A.d_hsml[p] = grad[3] * L;
+  float vp = 0.0f, vq = 0.0f;
+  for (int d = 0; d < 3; ++d) {
+    A.d_pos[p * pt.sp + d * pt.sc] = grad[d] * L;
+    vp = fmaxf(vp, (float)fabs(grad[d] * L));
+  }
+  for (int k = 0; k < pt.nq; ++k) {
+    A.d_q[p * pt.qsp + k * pt.qsk] = dqk[k];
+    vq = fmaxf(vq, (float)fabs(dqk[k]));
+  }
+  v[0] = vp;
+  v[1] = (float)fabs(grad[3] * L);
+  v[2] = (float)fabs(dm);
+  v[3] = (float)fabs(dr);
+  v[4] = (float)fabs(dw);
+  v[5] = vq;
+}
+
+// The largest magnitude of each output kind over a CTA's particles (each
+// warp's in vmax[warp], kept by its lane 0), added to the scales with one
+// atomic each.
+__device__ void flush_scales(const AdjArgs& A, float (*vmax)[kAdjScales]) {
+  __syncthreads();
+  if (threadIdx.x < kAdjScales) {
+    float m = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5) && w < 8; ++w) m = fmaxf(m, vmax[w][threadIdx.x]);
+    atomicMax(A.scale + threadIdx.x, __float_as_uint(m));  // non-negative floats order as their bits
+  }
+}
+
+// First pass.  FP64 path: every particle in FP64.  FP32 path: every
+// particle in FP32, except those the forward redoes in FP64 (done here in
+// FP64); a particle whose FP32 results miss the relative test is written
+// and queued for the second pass with its error estimates.
 template <int DIMS, int KERN>
-__global__ void __launch_bounds__(256) k_adj_particles(AdjArgs A) {
+__global__ void __launch_bounds__(256, 2) k_adj_particles(AdjArgs A) {
   const int lane = threadIdx.x & 31;
   const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const DevParticles& pt = A.pt;
-  const double L = A.mp.L;
   const int nq = pt.nq;
-  for (int64_t p = wid; p < pt.n; p += nw) {
+  __shared__ float vmax[8][kAdjScales];
+  if (lane == 0)
+    for (int c = 0; c < kAdjScales; ++c) vmax[(threadIdx.x >> 5) & 7][c] = 0.0f;
+  // every warp of the CTA runs the same number of rounds (the scales'
+  // block reduction waits for all of them)
+  const int64_t rounds = (pt.n + nw - 1) / nw;
+  for (int64_t it = 0; it < rounds; ++it) {
+    const int64_t p = wid + it * nw;
+    if (p >= pt.n) continue;
     PrepFP64 q;
     const int state = prep_particle_fp64<DIMS>(pt, A.mp, p, false, &q);
     double grad[4] = {0.0, 0.0, 0.0, 0.0};  // x, y, z, h (pixel units)
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
     if (state == kPrepMapped) {
-      if (!(A.g32 && adj_particle_fp32<DIMS, KERN>(A, p, q, lane, grad, dK, dqk)))
+      if (!(A.g32 && adj_particle_fp32<DIMS, KERN>(A, p, q, lane, grad, dK, dqk) != 0))
         adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
     }
     if (lane == 0) {
-      // K = w m L^3 / rho (2D), times L in 3D
-      const double LD = DIMS == 2 ? L * L * L : L * L * L * L;
-      const double m_in = state == kPrepMapped ? q.m_in : 0.0;
-      const double rho_in = state == kPrepMapped ? q.rho_in : 1.0;
-      const double w_in = state == kPrepMapped ? q.wgt : 0.0;
-      A.d_w[p] = dK * m_in * LD / rho_in;
-      A.d_mass[p] = dK * w_in * LD / rho_in;
-      A.d_rho[p] = -dK * w_in * m_in * LD / (rho_in * rho_in);
-      A.d_hsml[p] = grad[3] * L;
-      for (int d = 0; d < 3; ++d) A.d_pos[p * pt.sp + d * pt.sc] = grad[d] * L;
-      for (int k = 0; k < nq; ++k) A.d_q[p * pt.qsp + k * pt.qsk] = dqk[k];
+      float v[kAdjScales];
+      write_outputs<DIMS>(A, p, state, q, grad, dK, dqk, v);
+      float* vm = vmax[(threadIdx.x >> 5) & 7];
+      for (int c = 0; c < kAdjScales; ++c) vm[c] = fmaxf(vm[c], v[c]);
     }
   }
+  if (A.g32) flush_scales(A, vmax);
+}
+
+// Second pass (FP32 path): a queued particle keeps its FP32 results when
+// each error estimate is within kKeepRel of the larger of the value and
+// 1e-3 of the largest value of its kind; otherwise it is redone in FP64.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(256, 2) k_adj_pending(AdjArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const DevParticles& pt = A.pt;
+  const int nq = pt.nq;
+  const double L = A.mp.L;
+  const int64_t np = (int64_t)*A.n_pend;
+  float sc[kAdjScales];
+  for (int c = 0; c < kAdjScales; ++c) sc[c] = 1e-3f * __uint_as_float(A.scale[c]);
+  for (int64_t i = wid; i < np; i += nw) {
+    const AdjPending e = A.pend[i];
+    const int64_t p = e.p;
+    bool ok = true;
+    if (lane == 0) {
+      auto pass = [&](float err, double v, float s) { return err <= (float)kKeepRel * fmaxf((float)fabs(v), s); };
+      for (int d = 0; d < DIMS; ++d) ok = ok && pass(e.e[d], A.d_pos[p * pt.sp + d * pt.sc], sc[0]);
+      ok = ok && pass(e.e[3], A.d_hsml[p], sc[1]);
+      // dL/dK's error carried into w, m and rho by their factors
+      const double m_in = ld_elem(pt.attr_dtype, pt.mass, p), rho_in = ld_elem(pt.attr_dtype, pt.rho, p);
+      const double w_in = ld_elem(pt.attr_dtype, pt.w, p);
+      const double LD = DIMS == 2 ? L * L * L : L * L * L * L;
+      ok = ok && pass((float)(e.e[4] * fabs(w_in * LD / rho_in)), A.d_mass[p], sc[2]);
+      ok = ok && pass((float)(e.e[4] * fabs(w_in * m_in * LD / (rho_in * rho_in))), A.d_rho[p], sc[3]);
+      ok = ok && pass((float)(e.e[4] * fabs(m_in * LD / rho_in)), A.d_w[p], sc[4]);
+      for (int k = 0; k < nq && k < kAdjQ32; ++k) ok = ok && pass(e.e[5 + k], A.d_q[p * pt.qsp + k * pt.qsk], sc[5]);
+    }
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    if (ok) continue;  // warp-uniform
+    PrepFP64 q;
+    const int state = prep_particle_fp64<DIMS>(pt, A.mp, p, false, &q);
+    double grad[4] = {0.0, 0.0, 0.0, 0.0};
+    double dK = 0.0, dqk[kMaxQ];
+    for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
+    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
+    if (lane == 0) {
+      float v[kAdjScales];
+      write_outputs<DIMS>(A, p, state, q, grad, dK, dqk, v);
+    }
+  }
+}
+
+template <int DIMS, int KERN>
+void launch_adj_shape(const AdjArgs& A, int grid, cudaStream_t s) {
+  k_adj_particles<DIMS, KERN><<<grid, 256, 0, s>>>(A);
+  if (A.g32) k_adj_pending<DIMS, KERN><<<grid, 256, 0, s>>>(A);
 }
 
 template <int DIMS>
 void launch_adj_dims(int kernel, const AdjArgs& A, int grid, cudaStream_t s) {
   switch (kernel) {
-    case 0: k_adj_particles<DIMS, 0><<<grid, 256, 0, s>>>(A); break;
-    case 1: k_adj_particles<DIMS, 1><<<grid, 256, 0, s>>>(A); break;
-    case 2: k_adj_particles<DIMS, 2><<<grid, 256, 0, s>>>(A); break;
-    case 3: k_adj_particles<DIMS, 3><<<grid, 256, 0, s>>>(A); break;
-    default: k_adj_particles<DIMS, 4><<<grid, 256, 0, s>>>(A); break;
+    case 0: launch_adj_shape<DIMS, 0>(A, grid, s); break;
+    case 1: launch_adj_shape<DIMS, 1>(A, grid, s); break;
+    case 2: launch_adj_shape<DIMS, 2>(A, grid, s); break;
+    case 3: launch_adj_shape<DIMS, 3>(A, grid, s); break;
+    default: launch_adj_shape<DIMS, 4>(A, grid, s); break;
   }
 }
 
@@ -500,7 +630,7 @@ void launch_adj_dims(int kernel, const AdjArgs& A, int grid, cudaStream_t s) {
 cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParams& mp, const double* raw,
                            const double* grad_out, int mode, int reduce, double* gq, double* gw,
                            double* d_pos, double* d_hsml, double* d_mass, double* d_rho, double* d_w,
-                           double* d_q, float* g32, int num_sms, cudaStream_t s) {
+                           double* d_q, float* g32, void* scratch, int num_sms, cudaStream_t s) {
   const int dims = mp.dims;
   const int64_t P = mp.P;
   const int64_t PD = dims == 2 ? P * P : P * P * P;
@@ -522,6 +652,15 @@ cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParam
   A.d_w = d_w;
   A.d_q = d_q;
   A.st = nullptr;
+  A.scale = nullptr;
+  A.n_pend = nullptr;
+  A.pend = nullptr;
+  if (g32) {  // the second pass's scales, count and queue
+    A.scale = (unsigned*)scratch;
+    A.n_pend = A.scale + kAdjScales;
+    A.pend = (AdjPending*)((char*)scratch + 64);
+    cudaMemsetAsync(scratch, 0, 64, s);
+  }
   if (pt.n > 0) {
     int64_t grid = (pt.n + 7) / 8;
     if (grid > (int64_t)num_sms * 32) grid = (int64_t)num_sms * 32;
@@ -530,5 +669,7 @@ cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParam
   }
   return cudaGetLastError();
 }
+
+size_t adjoint_scratch_bytes(int64_t n) { return 64 + (size_t)(n > 0 ? n : 1) * sizeof(AdjPending); }
 
 }  // namespace sphg

@@ -47,7 +47,8 @@ void tiled_geometry(int dims, int64_t P, int tdim[3], int ntile[3], int64_t* n_t
 cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParams& mp, const double* raw,
                            const double* grad_out, int mode, int reduce, double* gq, double* gw,
                            double* d_pos, double* d_hsml, double* d_mass, double* d_rho, double* d_w,
-                           double* d_q, float* g32, int num_sms, cudaStream_t s);
+                           double* d_q, float* g32, void* scratch, int num_sms, cudaStream_t s);
+size_t adjoint_scratch_bytes(int64_t n);
 
 // K3 + K4 for one kernel shape (tiled_k<K>.cu).
 void launch_norm_deposit_0(const TiledArgs& A, int grid_rec, cudaStream_t s, cudaEvent_t* ev);
