@@ -38,6 +38,43 @@ __device__ __forceinline__ double wsum(double v) {
   return v;
 }
 
+__device__ __forceinline__ float wsumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// prep_particle_fp64 by lane 0, broadcast: the warp's lanes share one
+// particle, and FP64 is a small fraction of FP32 throughput on this GPU.
+// Every lane gets the state, the pixel coordinates, hsml, 1/hsml, the
+// kernel normalisation, the pixel ranges and scalar_zero; the factors
+// (area, col, vol, m, rho, w) stay on lane 0, which finishes the particle.
+template <int DIMS>
+__device__ __forceinline__ int prep_adj(const DevParticles& pt, const DevMapParams& mp, int64_t p, int lane,
+                                        PrepFP64* q) {
+  const unsigned full = 0xffffffffu;
+  PrepFP64 v;
+  v.x = v.y = v.z = v.hsml = v.h_inv = v.knorm = v.area = v.col = v.vol = v.m_in = v.rho_in = v.wgt = 0.0;
+  for (int d = 0; d < 3; ++d) v.lo[d] = v.hi[d] = 0;
+  v.scalar_zero = false;
+  int state = kPrepSkip;
+  if (lane == 0) state = prep_particle_fp64<DIMS>(pt, mp, p, false, &v);
+  *q = v;
+  state = __shfl_sync(full, state, 0);
+  q->x = __shfl_sync(full, v.x, 0);
+  q->y = __shfl_sync(full, v.y, 0);
+  q->z = __shfl_sync(full, v.z, 0);
+  q->hsml = __shfl_sync(full, v.hsml, 0);
+  q->h_inv = __shfl_sync(full, v.h_inv, 0);
+  q->knorm = __shfl_sync(full, v.knorm, 0);
+  for (int d = 0; d < 3; ++d) {
+    q->lo[d] = __shfl_sync(full, (long long)v.lo[d], 0);
+    q->hi[d] = __shfl_sync(full, (long long)v.hi[d], 0);
+  }
+  q->scalar_zero = __shfl_sync(full, v.scalar_zero ? 1 : 0, 0) != 0;
+  return state;
+}
+
 // Derivative of the un-normalised kernel shape, u < 1.
 template <int KERN>
 __device__ __forceinline__ double kshape_du(double u) {
@@ -318,6 +355,45 @@ constexpr float kTermEps = 5e-7f;
 constexpr float kEdgeEps = 6e-7f;
 constexpr double kKeepRel = 2e-5;
 
+// The FP32 path's finish of one particle by lane 0, from the warp sums
+// (S, sgg, sgd, sd, sq) and their rounding estimates (B: of sgg, then of
+// sgd; Bd of sd; Bq of sq): 1 when every result passes the relative test,
+// else 2 after queueing the particle for k_adj_pending with its errors in
+// output units (pos and hsml carry L, as the outputs do).
+template <int DIMS>
+__device__ __noinline__ int adj_finish32(const AdjArgs& A, int64_t p, const PrepFP64& q, double S, double sgg, double Gam1,
+                            const double* sgd, const double* sd, const double* sq, const double* B,
+                            const float* Bd, const float* Bq, double grad[4], double& dK, double* dqk) {
+  const int nq = A.pt.nq;
+  const double BG = B[0];
+  const double Gam = sgg / S;
+  const double relG = BG / fabs(sgg);  // relative error of Gam (S is a sum of positive terms)
+  bool keep = !(relG > kKeepRel);  // (0 / 0 when every term is 0: kept)
+  // sum (gam - Gam) dg = sum (gam - Gam1) dg - (Gam - Gam1) sum dg
+  const double dG = Gam - Gam1;
+  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
+  double val[4], err[4];
+  for (int t = 0; t < 4; ++t) {
+    val[t] = sgd[t] - dG * sd[t];
+    err[t] = B[1 + t] + fabs(dG) * (double)Bd[t] + fabs(Gam * sd[t]) * (sgg != 0.0 ? relG : 0.0);
+    if (err[t] > kKeepRel * fabs(val[t])) keep = false;
+  }
+  for (int k = 0; k < nq; ++k)
+    if ((double)Bq[k] > kKeepRel * fabs(sq[k])) keep = false;
+  dK = Gam;
+  for (int t = 0; t < 4; ++t) grad[t] = K / S * val[t];
+  for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
+  if (keep) return 1;
+  AdjPending e;
+  e.p = p;
+  for (int t = 0; t < 4; ++t) e.e[t] = (float)(fabs(K / S) * err[t] * A.mp.L);
+  e.e[4] = (float)(BG / S);
+  for (int k = 0; k < kAdjQ32; ++k) e.e[5 + k] = k < nq ? (float)(fabs(K / S) * (double)Bq[k]) : 0.0f;
+  e.pad = 0.0f;
+  A.pend[atomicAdd(A.n_pend, 1u)] = e;
+  return 2;
+}
+
 // One mapped particle on the FP32 path.  Returns 0 (nothing computed) for
 // the particles it leaves to the FP64 path, those the forward redoes in
 // FP64; 1 when every result passes the relative test (its rounding estimate
@@ -437,43 +513,19 @@ __device__ int adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q,
   }
   double sq[kAdjQ32];
   for (int k = 0; k < kAdjQ32; ++k) sq[k] = comp_total(aq[k], cq[k]);
-  // the rounding estimates: three times the root of the warp sums
-  const double BG = 3.0 * sqrt(wsum((double)bG));
-  double Bgd[4], Bd[4], Bq[kAdjQ32];
-  for (int t = 0; t < 4; ++t) {
-    Bgd[t] = 3.0 * sqrt(wsum((double)bgd[t]));
-    Bd[t] = 3.0 * sqrt(wsum((double)bd[t]));
-  }
-  for (int k = 0; k < kAdjQ32; ++k) Bq[k] = 3.0 * sqrt(wsum((double)bq[k]));
+  // the rounding estimates: three times the root of the warp sums (FP32:
+  // estimates of sums of squared FP32 term errors)
+  double B[9];
+  B[0] = 3.0 * sqrtf(wsumf(bG));
+  for (int t = 0; t < 4; ++t) B[1 + t] = 3.0 * sqrtf(wsumf(bgd[t]));
+  for (int t = 0; t < 4; ++t) bd[t] = 3.0f * sqrtf(wsumf(bd[t]));
+  for (int k = 0; k < kAdjQ32; ++k) bq[k] = 3.0f * sqrtf(wsumf(bq[k]));
   if (!(S > 0.0)) return 0;
-  const double Gam = sgg / S;
-  const double relG = BG / fabs(sgg);  // relative error of Gam (S is a sum of positive terms)
-  bool keep = !(relG > kKeepRel);  // (0 / 0 when every term is 0: kept)
-  // sum (gam - Gam) dg = sum (gam - Gam1) dg - (Gam - Gam1) sum dg
-  const double dG = Gam - (double)Gam1;
-  const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * A.mp.L;
-  double val[4], err[4];
-  for (int t = 0; t < 4; ++t) {
-    val[t] = sgd[t] - dG * sd[t];
-    err[t] = Bgd[t] + fabs(dG) * Bd[t] + fabs(Gam * sd[t]) * (sgg != 0.0 ? relG : 0.0);
-    if (err[t] > kKeepRel * fabs(val[t])) keep = false;
-  }
-  for (int k = 0; k < nq; ++k)
-    if (Bq[k] > kKeepRel * fabs(sq[k])) keep = false;
-  dK = Gam;
-  for (int t = 0; t < 4; ++t) grad[t] = K / S * val[t];
-  for (int k = 0; k < nq; ++k) dqk[k] = K / S * sq[k];
-  if (keep) return 1;  // warp-uniform: every value is a warp sum
-  if (lane == 0) {  // errors in output units: pos and hsml carry L, as the outputs do
-    AdjPending e;
-    e.p = p;
-    for (int t = 0; t < 4; ++t) e.e[t] = (float)(fabs(K / S) * err[t] * A.mp.L);
-    e.e[4] = (float)(BG / S);
-    for (int k = 0; k < kAdjQ32; ++k) e.e[5 + k] = k < nq ? (float)(fabs(K / S) * Bq[k]) : 0.0f;
-    e.pad = 0.0f;
-    A.pend[atomicAdd(A.n_pend, 1u)] = e;
-  }
-  return 2;
+  // the finish in FP64 by lane 0 (which writes the outputs), its verdict
+  // broadcast
+  int ret = 1;
+  if (lane == 0) ret = adj_finish32<DIMS>(A, p, q, S, sgg, (double)Gam1, sgd, sd, sq, B, bd, bq, grad, dK, dqk);
+  return __shfl_sync(0xffffffffu, ret, 0);
 }
 
 // Lane 0 writes particle p's derivatives (dK, grad in pixel units, dqk)
@@ -544,7 +596,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_particles(AdjArgs A) {
     const int64_t p = wid + it * nw;
     if (p >= pt.n) continue;
     PrepFP64 q;
-    const int state = prep_particle_fp64<DIMS>(pt, A.mp, p, false, &q);
+    const int state = prep_adj<DIMS>(pt, A.mp, p, lane, &q);
     double grad[4] = {0.0, 0.0, 0.0, 0.0};  // x, y, z, h (pixel units)
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
@@ -596,7 +648,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_pending(AdjArgs A) {
     ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     if (ok) continue;  // warp-uniform
     PrepFP64 q;
-    const int state = prep_particle_fp64<DIMS>(pt, A.mp, p, false, &q);
+    const int state = prep_adj<DIMS>(pt, A.mp, p, lane, &q);
     double grad[4] = {0.0, 0.0, 0.0, 0.0};
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
