@@ -355,16 +355,25 @@ constexpr float kTermEps = 5e-7f;
 constexpr float kEdgeEps = 6e-7f;
 constexpr double kKeepRel = 2e-5;
 
-// The FP32 path's finish of one particle by lane 0, from the warp sums
-// (S, sgg, sgd, sd, sq) and their rounding estimates (B: of sgg, then of
-// sgd; Bd of sd; Bq of sq): 1 when every result passes the relative test,
-// else 2 after queueing the particle for k_adj_pending with its errors in
-// output units (pos and hsml carry L, as the outputs do).
+// The warp sums of one particle on the FP32 path and their rounding
+// estimates (B: of sgg, then of the four sgd; Bd of sd; Bq of sq).
+struct Adj32Sums {
+  double S, sgg, Gam1, sgd[4], sd[4], sq[kAdjQ32], B[5];
+  float Bd[4], Bq[kAdjQ32];
+};
+
+// The FP32 path's finish of one particle, by the lane that holds the
+// particle (q: its own preparation, with the factors): 1 when every result
+// passes the relative test, else 2 after queueing the particle for
+// k_adj_pending with its errors in output units (pos and hsml carry L, as
+// the outputs do).
 template <int DIMS>
-__device__ __noinline__ int adj_finish32(const AdjArgs& A, int64_t p, const PrepFP64& q, double S, double sgg, double Gam1,
-                            const double* sgd, const double* sd, const double* sq, const double* B,
-                            const float* Bd, const float* Bq, double grad[4], double& dK, double* dqk) {
+__device__ __noinline__ int adj_finish32(const AdjArgs& A, int64_t p, const PrepFP64& q, const Adj32Sums& u,
+                                         double grad[4], double& dK, double* dqk) {
   const int nq = A.pt.nq;
+  const double S = u.S, sgg = u.sgg, Gam1 = u.Gam1;
+  const double *sgd = u.sgd, *sd = u.sd, *sq = u.sq, *B = u.B;
+  const float *Bd = u.Bd, *Bq = u.Bq;
   const double BG = B[0];
   const double Gam = sgg / S;
   const double relG = BG / fabs(sgg);  // relative error of Gam (S is a sum of positive terms)
@@ -394,16 +403,14 @@ __device__ __noinline__ int adj_finish32(const AdjArgs& A, int64_t p, const Prep
   return 2;
 }
 
-// One mapped particle on the FP32 path.  Returns 0 (nothing computed) for
-// the particles it leaves to the FP64 path, those the forward redoes in
-// FP64; 1 when every result passes the relative test (its rounding estimate
-// within kKeepRel of it); 2 when some result does not -- typically a
-// near-zero gradient whose terms cancel next to pixels of tiny W, where
-// dL/dW is large -- after lane 0 has queued the particle with its error
-// estimates for the second pass (k_adj_pending).
+// One mapped particle on the FP32 path, the warp over its footprint (q:
+// the particle's preparation, on every lane).  Returns 0 for the particles
+// it leaves to the FP64 path (those the forward redoes in FP64, maps of
+// more than kAdjQ32 quantities, footprints of 2^20 cells or more); else 1
+// after lane 0 has stored the warp sums and their rounding estimates in
+// *out for the particle's own lane to finish (adj_finish32).
 template <int DIMS, int KERN>
-__device__ int adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
-                                 double& dK, double* dqk) {
+__device__ int adj_fp32_sums(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, Adj32Sums* out) {
   const DevParticles& pt = A.pt;
   const int nq = pt.nq;
   if (nq > kAdjQ32) return 0;
@@ -515,17 +522,30 @@ __device__ int adj_particle_fp32(const AdjArgs& A, int64_t p, const PrepFP64& q,
   for (int k = 0; k < kAdjQ32; ++k) sq[k] = comp_total(aq[k], cq[k]);
   // the rounding estimates: three times the root of the warp sums (FP32:
   // estimates of sums of squared FP32 term errors)
-  double B[9];
-  B[0] = 3.0 * sqrtf(wsumf(bG));
-  for (int t = 0; t < 4; ++t) B[1 + t] = 3.0 * sqrtf(wsumf(bgd[t]));
-  for (int t = 0; t < 4; ++t) bd[t] = 3.0f * sqrtf(wsumf(bd[t]));
+  const float BG = 3.0f * sqrtf(wsumf(bG));
+  for (int t = 0; t < 4; ++t) {
+    bgd[t] = 3.0f * sqrtf(wsumf(bgd[t]));
+    bd[t] = 3.0f * sqrtf(wsumf(bd[t]));
+  }
   for (int k = 0; k < kAdjQ32; ++k) bq[k] = 3.0f * sqrtf(wsumf(bq[k]));
-  if (!(S > 0.0)) return 0;
-  // the finish in FP64 by lane 0 (which writes the outputs), its verdict
-  // broadcast
-  int ret = 1;
-  if (lane == 0) ret = adj_finish32<DIMS>(A, p, q, S, sgg, (double)Gam1, sgd, sd, sq, B, bd, bq, grad, dK, dqk);
-  return __shfl_sync(0xffffffffu, ret, 0);
+  if (!(S > 0.0)) return 0;  // warp-uniform
+  if (lane == 0) {
+    out->S = S;
+    out->sgg = sgg;
+    out->Gam1 = (double)Gam1;
+    out->B[0] = BG;
+    for (int t = 0; t < 4; ++t) {
+      out->sgd[t] = sgd[t];
+      out->sd[t] = sd[t];
+      out->B[1 + t] = bgd[t];
+      out->Bd[t] = bd[t];
+    }
+    for (int k = 0; k < kAdjQ32; ++k) {
+      out->sq[k] = sq[k];
+      out->Bq[k] = bq[k];
+    }
+  }
+  return 1;
 }
 
 // Lane 0 writes particle p's derivatives (dK, grad in pixel units, dqk)
@@ -575,10 +595,7 @@ __device__ void flush_scales(const AdjArgs& A, float (*vmax)[kAdjScales]) {
   }
 }
 
-// First pass.  FP64 path: every particle in FP64.  FP32 path: every
-// particle in FP32, except those the forward redoes in FP64 (done here in
-// FP64); a particle whose FP32 results miss the relative test is written
-// and queued for the second pass with its error estimates.
+// The FP64 path: every particle in FP64, a warp each.
 template <int DIMS, int KERN>
 __global__ void __launch_bounds__(256, 2) k_adj_particles(AdjArgs A) {
   const int lane = threadIdx.x & 31;
@@ -586,32 +603,97 @@ __global__ void __launch_bounds__(256, 2) k_adj_particles(AdjArgs A) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const DevParticles& pt = A.pt;
   const int nq = pt.nq;
-  __shared__ float vmax[8][kAdjScales];
-  if (lane == 0)
-    for (int c = 0; c < kAdjScales; ++c) vmax[(threadIdx.x >> 5) & 7][c] = 0.0f;
-  // every warp of the CTA runs the same number of rounds (the scales'
-  // block reduction waits for all of them)
-  const int64_t rounds = (pt.n + nw - 1) / nw;
-  for (int64_t it = 0; it < rounds; ++it) {
-    const int64_t p = wid + it * nw;
-    if (p >= pt.n) continue;
+  for (int64_t p = wid; p < pt.n; p += nw) {
     PrepFP64 q;
     const int state = prep_adj<DIMS>(pt, A.mp, p, lane, &q);
     double grad[4] = {0.0, 0.0, 0.0, 0.0};  // x, y, z, h (pixel units)
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
-    if (state == kPrepMapped) {
-      if (!(A.g32 && adj_particle_fp32<DIMS, KERN>(A, p, q, lane, grad, dK, dqk) != 0))
-        adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
-    }
+    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
     if (lane == 0) {
       float v[kAdjScales];
       write_outputs<DIMS>(A, p, state, q, grad, dK, dqk, v);
-      float* vm = vmax[(threadIdx.x >> 5) & 7];
-      for (int c = 0; c < kAdjScales; ++c) vm[c] = fmaxf(vm[c], v[c]);
     }
   }
-  if (A.g32) flush_scales(A, vmax);
+}
+
+// First pass of the FP32 path, a warp per group of 32 particles: the lanes
+// prepare their particles side by side (FP64, one particle each, into
+// shared memory), the warp sums each particle's footprint in FP32 (or does
+// it in FP64 where the forward would), and the lanes finish their particles
+// side by side again (FP64), so the per-particle FP64 work -- a small
+// fraction of FP32 throughput on this GPU -- costs one warp instruction
+// stream per 32 particles.  A particle whose FP32 results miss the relative
+// test is written and queued for the second pass.  Maps of at most
+// kAdjQ32 quantities; four warps per CTA, so a group's preparations and
+// sums fit in static shared memory.
+template <int DIMS, int KERN>
+__global__ void __launch_bounds__(128, 4) k_adj_particles32(AdjArgs A) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = (threadIdx.x >> 5) & 3;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const DevParticles& pt = A.pt;
+  const int nq = pt.nq;
+  __shared__ PrepFP64 qs[4][32];
+  __shared__ Adj32Sums sums[4][32];
+  __shared__ float vmax[8][kAdjScales];
+  float vm[kAdjScales] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  const int64_t ngroups = (pt.n + 31) / 32;
+  // every warp of the CTA runs the same number of rounds (the scales'
+  // block reduction waits for all of them)
+  const int64_t rounds = (ngroups + nw - 1) / nw;
+  for (int64_t it = 0; it < rounds; ++it) {
+    const int64_t g = wid + it * nw;
+    if (g >= ngroups) continue;
+    const int64_t g0 = g * 32;
+    const int cnt = pt.n - g0 < 32 ? (int)(pt.n - g0) : 32;
+    const int64_t pm = g0 + lane;
+    int stm = kPrepSkip;
+    {
+      PrepFP64 v;
+      v.x = v.y = v.z = v.hsml = v.h_inv = v.knorm = v.area = v.col = v.vol = 0.0;
+      v.m_in = v.rho_in = v.wgt = 0.0;
+      for (int d = 0; d < 3; ++d) v.lo[d] = v.hi[d] = 0;
+      v.scalar_zero = false;
+      if (lane < cnt) stm = prep_particle_fp64<DIMS>(pt, A.mp, pm, false, &v);
+      qs[warp][lane] = v;
+    }
+    __syncwarp();
+    double gm[4] = {0.0, 0.0, 0.0, 0.0}, dKm = 0.0, dqm[kAdjQ32] = {0.0, 0.0, 0.0, 0.0};
+    int mode = 0;  // 1: sums of this lane's particle in sums[warp][lane]; 2: results in gm, dKm, dqm
+    for (int j = 0; j < cnt; ++j) {
+      if (__shfl_sync(full, stm, j) != kPrepMapped) continue;  // warp-uniform
+      const PrepFP64& qj = qs[warp][j];
+      if (adj_fp32_sums<DIMS, KERN>(A, g0 + j, qj, lane, &sums[warp][j])) {
+        if (lane == j) mode = 1;
+      } else {
+        double grad[4] = {0.0, 0.0, 0.0, 0.0}, dK = 0.0, dqk[kMaxQ];
+        for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
+        adj_particle_fp64<DIMS, KERN>(A, g0 + j, qj, lane, grad, dK, dqk);
+        if (lane == j) {
+          for (int t = 0; t < 4; ++t) gm[t] = grad[t];
+          dKm = dK;
+          for (int k = 0; k < nq; ++k) dqm[k] = dqk[k];
+          mode = 2;
+        }
+      }
+    }
+    __syncwarp();  // lane 0 stored the sums that their own lanes finish
+    if (mode == 1) adj_finish32<DIMS>(A, pm, qs[warp][lane], sums[warp][lane], gm, dKm, dqm);
+    if (lane < cnt) {
+      float v[kAdjScales];
+      write_outputs<DIMS>(A, pm, stm, qs[warp][lane], gm, dKm, dqm, v);
+      for (int c = 0; c < kAdjScales; ++c) vm[c] = fmaxf(vm[c], v[c]);
+    }
+    __syncwarp();  // qs[warp] and sums[warp] are rewritten by the next group
+  }
+  for (int c = 0; c < kAdjScales; ++c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vm[c] = fmaxf(vm[c], __shfl_xor_sync(full, vm[c], o));
+    if (lane == 0) vmax[warp][c] = vm[c];
+  }
+  flush_scales(A, vmax);
 }
 
 // Second pass (FP32 path): a queued particle keeps its FP32 results when
@@ -661,19 +743,23 @@ __global__ void __launch_bounds__(256, 2) k_adj_pending(AdjArgs A) {
 }
 
 template <int DIMS, int KERN>
-void launch_adj_shape(const AdjArgs& A, int grid, cudaStream_t s) {
-  k_adj_particles<DIMS, KERN><<<grid, 256, 0, s>>>(A);
-  if (A.g32) k_adj_pending<DIMS, KERN><<<grid, 256, 0, s>>>(A);
+void launch_adj_shape(const AdjArgs& A, int grid, int grid32, cudaStream_t s) {
+  if (A.g32 && A.pt.nq <= kAdjQ32) {  // more quantities: every particle in FP64
+    k_adj_particles32<DIMS, KERN><<<grid32, 128, 0, s>>>(A);
+    k_adj_pending<DIMS, KERN><<<grid, 256, 0, s>>>(A);
+  } else {
+    k_adj_particles<DIMS, KERN><<<grid, 256, 0, s>>>(A);
+  }
 }
 
 template <int DIMS>
-void launch_adj_dims(int kernel, const AdjArgs& A, int grid, cudaStream_t s) {
+void launch_adj_dims(int kernel, const AdjArgs& A, int grid, int grid32, cudaStream_t s) {
   switch (kernel) {
-    case 0: launch_adj_shape<DIMS, 0>(A, grid, s); break;
-    case 1: launch_adj_shape<DIMS, 1>(A, grid, s); break;
-    case 2: launch_adj_shape<DIMS, 2>(A, grid, s); break;
-    case 3: launch_adj_shape<DIMS, 3>(A, grid, s); break;
-    default: launch_adj_shape<DIMS, 4>(A, grid, s); break;
+    case 0: launch_adj_shape<DIMS, 0>(A, grid, grid32, s); break;
+    case 1: launch_adj_shape<DIMS, 1>(A, grid, grid32, s); break;
+    case 2: launch_adj_shape<DIMS, 2>(A, grid, grid32, s); break;
+    case 3: launch_adj_shape<DIMS, 3>(A, grid, grid32, s); break;
+    default: launch_adj_shape<DIMS, 4>(A, grid, grid32, s); break;
   }
 }
 
@@ -716,8 +802,11 @@ cudaError_t launch_adjoint(int kernel, const DevParticles& pt, const DevMapParam
   if (pt.n > 0) {
     int64_t grid = (pt.n + 7) / 8;
     if (grid > (int64_t)num_sms * 32) grid = (int64_t)num_sms * 32;
-    if (dims == 2) launch_adj_dims<2>(kernel, A, (int)grid, s);
-    else launch_adj_dims<3>(kernel, A, (int)grid, s);
+    // FP32 first pass: a warp per 32 particles, four warps per CTA
+    int64_t grid32 = (pt.n + 127) / 128;
+    if (grid32 > (int64_t)num_sms * 32) grid32 = (int64_t)num_sms * 32;
+    if (dims == 2) launch_adj_dims<2>(kernel, A, (int)grid, (int)grid32, s);
+    else launch_adj_dims<3>(kernel, A, (int)grid, (int)grid32, s);
   }
   return cudaGetLastError();
 }
