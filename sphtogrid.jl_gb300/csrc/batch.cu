@@ -252,6 +252,8 @@ struct sphg_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;  // own stream (capture and synchronous work)
+  cudaStream_t side = nullptr;    // second stream: renormalisation shapes run side by side
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaStream_t last = nullptr;    // stream of the last launch
   std::vector<sphg::DevStatus> h_status;
   std::string err;
@@ -495,9 +497,23 @@ int enqueue(sphg_batch* b, cudaStream_t s) {
   for (const auto& z : p.zero) BCK(cudaMemsetAsync(z.first, 0, z.second, s));
   kb_prep<<<p.k1_grid, 256, 0, s>>>(p.dev);
   kb_scan<<<nm, 1024, 0, s>>>(p.dev);
-  for (const int shape : p.shapes) {  // dims * 8 + kernel shape
-    if (shape >> 3 == 2) launch_norm_dims<2>(shape & 7, p.dev, b->num_sms, s);
-    else launch_norm_dims<3>(shape & 7, p.dev, b->num_sms, s);
+  // the renormalisation of each (dimensions, kernel shape) touches only its
+  // own maps: the shapes after the first run on the side stream, so one
+  // shape's tail overlaps another's work; the deposit waits for both
+  const bool two = p.shapes.size() > 1;
+  if (two) {
+    BCK(cudaEventRecord(b->fork, s));
+    BCK(cudaStreamWaitEvent(b->side, b->fork, 0));
+  }
+  for (size_t i = 0; i < p.shapes.size(); ++i) {  // dims * 8 + kernel shape
+    const int shape = p.shapes[i];
+    cudaStream_t t = (two && i > 0) ? b->side : s;
+    if (shape >> 3 == 2) launch_norm_dims<2>(shape & 7, p.dev, b->num_sms, t);
+    else launch_norm_dims<3>(shape & 7, p.dev, b->num_sms, t);
+  }
+  if (two) {
+    BCK(cudaEventRecord(b->join, b->side));
+    BCK(cudaStreamWaitEvent(s, b->join, 0));
   }
   if (!launch_kb_deposit(p.tile_x, p.tile_y, p.dev, p.det, b->num_sms * p.ctas_per_sm, p.smem, s))
     return bfail(b, SPHG_ERR_ARG, "tile shape must be 16x16, 32x16 or 32x32");
@@ -629,7 +645,10 @@ int sphg_batch_create(sphg_context* ctx, int32_t n_maps, const sphg_map_desc* de
     if (int st = sphg_mapping_parameters(xl, yl, zl, c0, -1.0, -1.0, -1.0, -1.0, Pm, D.par.boxsize, &M.cpar))
       return done(bfail(b, st, who + "parameters"));
   }
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess)
     return done(bfail(b, SPHG_ERR_CUDA, "stream"));
   // tuning candidates (tile shape, deposit CTAs per SM, large-footprint threshold)
   struct Cand {
@@ -765,7 +784,11 @@ int sphg_batch_destroy(sphg_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   sphg::free_plan(b->plan);
+  if (b->side) cudaStreamSynchronize(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->side) cudaStreamDestroy(b->side);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   delete b;
   return SPHG_OK;
 }
