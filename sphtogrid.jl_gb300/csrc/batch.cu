@@ -54,15 +54,17 @@ __device__ __forceinline__ int find_seg_i(const int* base, int n, int x) {
   return lo;
 }
 
-constexpr int64_t kOneIteration = (int64_t)1 << 62;
+// Particles of one map per K1 CTA (four rounds of 256 threads): the CTA's
+// set-up (its map, the shared tile counts) is paid once per 1024 particles.
+constexpr int64_t kPrepSpan = 1024;
 
 __global__ void __launch_bounds__(256, 4) kb_prep(BatchDev B) {
   const int m = find_seg_i(B.blk_base, B.n_maps, blockIdx.x);
   const TiledArgs& A = B.maps[m];
-  const int64_t base = (int64_t)(blockIdx.x - B.blk_base[m]) * blockDim.x;
+  const int64_t base = (int64_t)(blockIdx.x - B.blk_base[m]) * kPrepSpan;
   __shared__ PrepShared sh;
-  if (A.mp.dims == 2) prep_count<2>(A, base, kOneIteration, sh);
-  else prep_count<3>(A, base, kOneIteration, sh);
+  if (A.mp.dims == 2) prep_count<2>(A, base, blockDim.x, sh, base + kPrepSpan);
+  else prep_count<3>(A, base, blockDim.x, sh, base + kPrepSpan);
 }
 
 __global__ void __launch_bounds__(1024) kb_scan(BatchDev B) {
@@ -367,7 +369,7 @@ int build_plan(sphg_batch* b) {
   for (int m = 0; m < nm; ++m) {
     const BatchMapHost& M = b->maps[m];
     const int64_t n = M.desc.parts.n;
-    p.blk_base[m + 1] = p.blk_base[m] + (int)std::max<int64_t>(1, (n + 255) / 256);
+    p.blk_base[m + 1] = p.blk_base[m] + (int)std::max<int64_t>(1, (n + kPrepSpan - 1) / kPrepSpan);
   }
   for (int i = 0; i < nm; ++i) {
     const BatchMapHost& M = b->maps[p.order[i]];

@@ -60,7 +60,8 @@ __device__ __forceinline__ bool factors_f32(const DevMapParams& mp, const PrepLi
 }
 
 // K1 body: this CTA's threads take particles base0 + threadIdx.x, then
-// every `stride` further (a whole CTA enters each iteration together).
+// every `stride` further, below `end` (a whole CTA enters each iteration
+// together).
 struct PrepShared {
   int hist[kTileHist];  // overlaps per tile (maps of few tiles)
   int list[kTileHist];  // tiles touched by this CTA, once each
@@ -68,7 +69,8 @@ struct PrepShared {
 };
 
 template <int DIMS>
-__device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, PrepShared& sh) {
+__device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, PrepShared& sh,
+                           int64_t end = INT64_MAX) {
   int* const s_hist = sh.hist;
   int* const s_list = sh.list;
   const bool hist = A.n_tiles <= kTileHist;  // uniform across the CTA
@@ -81,7 +83,8 @@ __device__ void prep_count(const TiledArgs& A, int64_t base0, int64_t stride, Pr
   unsigned long long c_mapped = 0, c_dep = 0;
   double c_pm = 0.0;
   unsigned flags = 0;
-  for (int64_t base = base0; base < A.pt.n; base += stride) {
+  const int64_t stop = end < A.pt.n ? end : A.pt.n;
+  for (int64_t base = base0; base < stop; base += stride) {
     const int64_t p = base + threadIdx.x;
     PrepLite q;
     int state = kPrepSkip;
