@@ -212,10 +212,19 @@ struct AdjArgs {
 constexpr int kAdjQ32 = 4;
 
 // One mapped particle in FP64 (the warp's lanes stride over its footprint):
-// grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.
+// grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.  u is the forward's
+// (sqrt(r^2) / h as r * (1/h), cell_fp64), so the cells in the support are
+// the forward's.  The forward's branch -- the fallback g = A where its
+// renormalisation sum is zero -- is settled inside the pass that gathers the
+// sums: a cell with u < 1 at positive overlap has a positive term (every
+// kernel shape is positive below u = 1, at least (2^-53)^10 there), and with
+// no negative overlap in the support the sum is then positive.  Only a
+// particle without such a cell (sub-pixel ones) runs the sum as a pass of its
+// own, and the sums again on its branch.
 template <int DIMS, int KERN>
 __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
                                   double& dK, double* dqk) {
+  const unsigned full = 0xffffffffu;
   const DevParticles& pt = A.pt;
   const double L = A.mp.L;
   const int64_t P = A.mp.P;
@@ -224,82 +233,91 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
   const int64_t ni = q.hi[0] - iMin + 1, nj = q.hi[1] - jMin + 1, nk = q.hi[2] - kMin + 1;
   const int64_t njk = nj * nk, F = ni * njk;
   const double xs[3] = {q.x, q.y, q.z};
-  const double h = q.hsml;
-  // pass 1: renormalisation sum and branch (as the forward)
-  double s_w = 0.0;
-  for (int64_t f = lane; f < F; f += 32) {
-    const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
-    double u, a;
-    cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &u, &a);
-    if (u <= 1.0) s_w += kshape<KERN, double>(u) * a;
-  }
-  s_w = wsum(s_w);
-  const bool fallback = (s_w == 0.0);
-  // pass 2: recompute g and its derivatives, gather the image gradients
-  double S = 0.0, sgg = 0.0, sgd[4] = {0, 0, 0, 0}, sd[4] = {0, 0, 0, 0}, sq[kMaxQ];
-  for (int k = 0; k < nq; ++k) sq[k] = 0.0;
-  for (int64_t f = lane; f < F; f += 32) {
-    const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
-    const int64_t cell[3] = {iMin + ia, jMin + jb, kMin + kc};
-    double dist[3] = {0, 0, 0}, ov[3] = {1, 1, 1}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
-    for (int d = 0; d < DIMS; ++d) {
-      cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
-      const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
-      const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
-      dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
-      doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
-    }
-    const double A_ = ov[0] * ov[1] * ov[2];
-    double dA[4];
-    dA[3] = 0.0;
-    for (int d = 0; d < 3; ++d) {
-      double rest = 1.0;
-      for (int e = 0; e < 3; ++e)
-        if (e != d) rest *= ov[e];
-      dA[d] = d < DIMS ? dox[d] * rest : 0.0;
-      if (d < DIMS) dA[3] += doh[d] * rest;
-    }
-    const double r2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
-    const double rr = sqrt(r2);
-    const double u = rr / h;
-    double g, dg[4];
-    if (fallback) {
-      g = A_;
-      for (int t = 0; t < 4; ++t) dg[t] = dA[t];
-    } else if (u <= 1.0) {
-      const double s = kshape<KERN, double>(u), sp = kshape_du<KERN>(u);
-      g = s * A_;
-      for (int d = 0; d < 3; ++d) {
-        const double du = (d < DIMS && rr > 0.0) ? dist[d] / (rr * h) : 0.0;
-        dg[d] = sp * du * A_ + s * dA[d];
+  const double h = q.hsml, h_inv = q.h_inv;
+  double S, sgg, sgd[4], sd[4], sq[kMaxQ];
+  bool fallback = false, decided = false;
+  for (;;) {
+    S = sgg = 0.0;
+    for (int t = 0; t < 4; ++t) sgd[t] = sd[t] = 0.0;
+    for (int k = 0; k < nq; ++k) sq[k] = 0.0;
+    bool pos_term = false, neg_term = false;
+    for (int64_t f = lane; f < F; f += 32) {
+      const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
+      const int64_t cell[3] = {iMin + ia, jMin + jb, kMin + kc};
+      double dist[3] = {0, 0, 0}, ov[3] = {1, 1, 1}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
+      for (int d = 0; d < DIMS; ++d) {
+        cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
+        const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
+        const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
+        dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
+        doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
       }
-      dg[3] = sp * (-u / h) * A_ + s * dA[3];
-    } else {
-      g = 0.0;
-      dg[0] = dg[1] = dg[2] = dg[3] = 0.0;
+      const double A_ = ov[0] * ov[1] * ov[2];
+      double dA[4];
+      dA[3] = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        double rest = 1.0;
+        for (int e = 0; e < 3; ++e)
+          if (e != d) rest *= ov[e];
+        dA[d] = d < DIMS ? dox[d] * rest : 0.0;
+        if (d < DIMS) dA[3] += doh[d] * rest;
+      }
+      const double r2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
+      const double rr = sqrt(r2);
+      const double u = rr * h_inv;
+      if (u <= 1.0) {
+        pos_term = pos_term || (u < 1.0 && A_ > 0.0);
+        neg_term = neg_term || A_ < 0.0;
+      }
+      double g, dg[4];
+      if (fallback) {
+        g = A_;
+        for (int t = 0; t < 4; ++t) dg[t] = dA[t];
+      } else if (u <= 1.0) {
+        const double s = kshape<KERN, double>(u), sp = kshape_du<KERN>(u);
+        const double irh = rr > 0.0 ? h_inv / rr : 0.0;  // du/dx_d = dist_d / (r h)
+        g = s * A_;
+        for (int d = 0; d < 3; ++d) dg[d] = sp * (dist[d] * irh) * A_ + s * dA[d];
+        dg[3] = sp * (-u * h_inv) * A_ + s * dA[3];
+      } else {
+        g = 0.0;
+        dg[0] = dg[1] = dg[2] = dg[3] = 0.0;
+      }
+      const int64_t idx = DIMS == 2 ? cell[0] * P + cell[1] : (cell[0] * P + cell[1]) * P + cell[2];
+      double gam = A.gw[idx];
+      for (int k = 0; k < nq; ++k) {
+        const double gqk = A.gq[k * A.PD + idx];
+        const double qk = q.scalar_zero ? 0.0 : ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk);
+        gam += qk * gqk;
+        sq[k] += g * gqk;
+      }
+      S += g;
+      sgg += gam * g;
+      for (int t = 0; t < 4; ++t) {
+        sgd[t] += gam * dg[t];
+        sd[t] += dg[t];
+      }
     }
-    const int64_t idx = DIMS == 2 ? cell[0] * P + cell[1] : (cell[0] * P + cell[1]) * P + cell[2];
-    double gam = A.gw[idx];
-    for (int k = 0; k < nq; ++k) {
-      const double gqk = A.gq[k * A.PD + idx];
-      const double qk = q.scalar_zero ? 0.0 : ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk);
-      gam += qk * gqk;
-      sq[k] += g * gqk;
-    }
-    S += g;
-    sgg += gam * g;
+    S = wsum(S);
+    sgg = wsum(sgg);
     for (int t = 0; t < 4; ++t) {
-      sgd[t] += gam * dg[t];
-      sd[t] += dg[t];
+      sgd[t] = wsum(sgd[t]);
+      sd[t] = wsum(sd[t]);
     }
+    for (int k = 0; k < nq; ++k) sq[k] = wsum(sq[k]);
+    if (decided || (__any_sync(full, pos_term) && !__any_sync(full, neg_term))) break;
+    // the forward's renormalisation sum as a pass of its own, then the sums
+    // again (recomputed rather than kept live across that pass)
+    double s_w = 0.0;
+    for (int64_t f = lane; f < F; f += 32) {
+      const int64_t ia = f / njk, r = f - ia * njk, jb = r / nk, kc = r - jb * nk;
+      double uc, a;
+      cell_fp64<DIMS>(q, iMin + ia, jMin + jb, kMin + kc, &uc, &a);
+      if (uc <= 1.0) s_w += kshape<KERN, double>(uc) * a;
+    }
+    fallback = wsum(s_w) == 0.0;
+    decided = true;
   }
-  S = wsum(S);
-  sgg = wsum(sgg);
-  for (int t = 0; t < 4; ++t) {
-    sgd[t] = wsum(sgd[t]);
-    sd[t] = wsum(sd[t]);
-  }
-  for (int k = 0; k < nq; ++k) sq[k] = wsum(sq[k]);
   const double K = DIMS == 2 ? q.area * q.wgt * q.col : q.vol * q.wgt * L;
   if (S > 0.0) {
     const double Gam = sgg / S;
