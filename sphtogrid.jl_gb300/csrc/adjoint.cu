@@ -213,14 +213,18 @@ constexpr int kAdjQ32 = 4;
 
 // One mapped particle in FP64 (the warp's lanes stride over its footprint):
 // grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.  u is the forward's
-// (sqrt(r^2) / h as r * (1/h), cell_fp64), so the cells in the support are
-// the forward's.  The forward's branch -- the fallback g = A where its
-// renormalisation sum is zero -- is settled inside the pass that gathers the
-// sums: a cell with u < 1 at positive overlap has a positive term (every
-// kernel shape is positive below u = 1, at least (2^-53)^10 there), and with
-// no negative overlap in the support the sum is then positive.  Only a
+// to a few ulp (cell_fp64 forms sqrt(r^2) * (1/h)); a cell it moves across
+// u = 1 has a weight and a derivative of order (1 - u)^2 or less, nil.  The
+// forward's branch -- the fallback g = A where its renormalisation sum is
+// zero -- is settled inside the pass that gathers the sums: a cell with
+// u < kSureU (so the forward's u < 1) at positive overlap has a positive
+// term (every kernel shape is positive below u = 1, at least (2^-53)^10
+// there), and with no negative overlap in the footprint the sum is then
+// positive.  Only a
 // particle without such a cell (sub-pixel ones) runs the sum as a pass of its
 // own, and the sums again on its branch.
+constexpr double kSureU = 0.9999999;
+
 template <int DIMS, int KERN>
 __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
                                   double& dK, double* dqk) {
@@ -262,22 +266,24 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
         dA[d] = d < DIMS ? dox[d] * rest : 0.0;
         if (d < DIMS) dA[3] += doh[d] * rest;
       }
-      const double r2 = dist[0] * dist[0] + dist[1] * dist[1] + dist[2] * dist[2];
-      const double rr = sqrt(r2);
-      const double u = rr * h_inv;
-      if (u <= 1.0) {
-        pos_term = pos_term || (u < 1.0 && A_ > 0.0);
-        neg_term = neg_term || A_ < 0.0;
-      }
+      double r2 = dist[0] * dist[0] + dist[1] * dist[1];
+      if (DIMS == 3) r2 += dist[2] * dist[2];
+      // r and 1/r from one reciprocal square root (1 ulp), so u is within a
+      // few ulp of the forward's
+      const double rs = r2 > 0.0 ? rsqrt(r2) : 0.0;
+      const double u = r2 * rs * h_inv;
+      pos_term = pos_term || (u < kSureU && A_ > 0.0);
+      neg_term = neg_term || A_ < 0.0;
       double g, dg[4];
       if (fallback) {
         g = A_;
         for (int t = 0; t < 4; ++t) dg[t] = dA[t];
       } else if (u <= 1.0) {
         const double s = kshape<KERN, double>(u), sp = kshape_du<KERN>(u);
-        const double irh = rr > 0.0 ? h_inv / rr : 0.0;  // du/dx_d = dist_d / (r h)
+        const double irh = rs * h_inv;  // du/dx_d = dist_d / (r h)
         g = s * A_;
-        for (int d = 0; d < 3; ++d) dg[d] = sp * (dist[d] * irh) * A_ + s * dA[d];
+        for (int d = 0; d < DIMS; ++d) dg[d] = sp * (dist[d] * irh) * A_ + s * dA[d];
+        if (DIMS == 2) dg[2] = 0.0;
         dg[3] = sp * (-u * h_inv) * A_ + s * dA[3];
       } else {
         g = 0.0;
@@ -294,6 +300,7 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
       S += g;
       sgg += gam * g;
       for (int t = 0; t < 4; ++t) {
+        if (DIMS == 2 && t == 2) continue;
         sgd[t] += gam * dg[t];
         sd[t] += dg[t];
       }
@@ -301,6 +308,7 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
     S = wsum(S);
     sgg = wsum(sgg);
     for (int t = 0; t < 4; ++t) {
+      if (DIMS == 2 && t == 2) continue;
       sgd[t] = wsum(sgd[t]);
       sd[t] = wsum(sd[t]);
     }
