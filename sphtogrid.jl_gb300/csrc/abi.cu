@@ -882,9 +882,10 @@ int sphg_adjoint(sphg_context* ctx, const sphg_params* par, const sphg_options* 
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   Carve cv;
   const size_t o_g = cv.take((size_t)PD * (nq + 1) * sizeof(double));
-  // FP32C: the image gradients in FP32 too, for the FP32 per-cell path
+  // FP32C: the image gradients as FP32 (hi, lo) pairs too, for the FP32
+  // per-cell path
   const bool f32 = opt->precision == SPHG_PREC_FP32C;
-  const size_t o_g32 = f32 ? cv.take((size_t)PD * (nq + 1) * sizeof(float)) : 0;
+  const size_t o_g32 = f32 ? cv.take((size_t)PD * (nq + 1) * 2 * sizeof(float)) : 0;
   const size_t o_adj = f32 ? cv.take(sphg::adjoint_scratch_bytes(n)) : 0;
   if (int st = ensure_ws(ctx, cv.off, s)) return st;
   double* gq = (double*)((char*)ctx->ws + o_g);

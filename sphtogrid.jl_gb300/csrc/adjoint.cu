@@ -137,7 +137,9 @@ __device__ __forceinline__ float kshape_du_f(float u) {
 }
 
 // dL/d(out) -> dL/dQ_k, dL/dW in raw row order (row = i*P + j or i*P^2 + j*P + k);
-// g32 (FP32 path): the same [nq][PD] then [PD], in FP32.
+// g32 (FP32 path): the same [nq][PD] then [PD] as FP32 (hi, lo) pairs, the
+// nq + 1 planes of hi = float(v) and then the nq + 1 planes of
+// lo = float(v - hi), so hi + lo carries v to about 48 bits.
 __global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ raw, const double* __restrict__ g,
                                                      int dims, int64_t P, int nq, int mode, int reduce,
                                                      double* __restrict__ gq, double* __restrict__ gw,
@@ -174,8 +176,13 @@ __global__ void __launch_bounds__(256) k_adj_reduce(const double* __restrict__ r
     }
     gw[row] = dw;
     if (g32) {
-      for (int c = 0; c < nq; ++c) g32[row + c * PD] = (float)gq[row + c * PD];
-      g32[row + (int64_t)nq * PD] = (float)dw;
+      const int64_t LO = (int64_t)(nq + 1) * PD;
+      for (int c = 0; c <= nq; ++c) {
+        const double v = c < nq ? gq[row + c * PD] : dw;
+        const float hv = (float)v;
+        g32[row + c * PD] = hv;
+        g32[LO + row + c * PD] = (float)(v - (double)hv);
+      }
     }
   }
 }
@@ -197,7 +204,7 @@ struct AdjArgs {
   DevMapParams mp;
   const double* gq;  // [nq][PD]
   const double* gw;  // [PD]
-  const float* g32;  // FP32 path: gq then gw in FP32, or NULL (FP64 throughout)
+  const float* g32;  // FP32 path: gq then gw as FP32 (hi, lo) planes, or NULL (FP64 throughout)
   int64_t PD;
   double* d_pos;     // strides of pt.pos
   double *d_hsml, *d_mass, *d_rho, *d_w;
@@ -368,8 +375,11 @@ __device__ __forceinline__ void axis_terms_f(float f, float h, int a, float& dis
 }
 
 // Error estimate of the FP32 path.  The image gradient gam = dL/dW +
-// sum_k q_k dL/dQ_k is formed in FP64 per cell (its parts cancel where q is
-// near the map value) and rounded once.  A per-cell weight or derivative
+// sum_k q_k dL/dQ_k is formed per cell from FP32 (hi, lo) pairs of its
+// factors with exact products (FMA) and exact sums (TwoSum), about 48 bits
+// (its parts cancel where q is near the map value), and rounded once; the
+// error of that formation stays below kGamEps (|dL/dW| + sum_k |q_k dL/dQ_k|)
+// and is added to each term's.  A per-cell weight or derivative
 // carries a relative rounding error of about kTermEps (a few tens of FP32
 // operations), amplified near the kernel edge, where (1 - u)^k turns the
 // rounding of u into kEdgeEps / (1 - u).  The terms' errors are independent,
@@ -380,6 +390,7 @@ __device__ __forceinline__ void axis_terms_f(float f, float h, int a, float& dis
 constexpr float kTermEps = 5e-7f;
 constexpr float kEdgeEps = 6e-7f;
 constexpr double kKeepRel = 2e-5;
+constexpr float kGamEps = 9.1e-13f;  // 2^-40: representation, cross products, low-part sums
 
 // The warp sums of one particle on the FP32 path and their rounding
 // estimates (B: of sgg, then of the four sgd; Bd of sd; Bq of sq).
@@ -448,20 +459,31 @@ __device__ int adj_fp32_sums(const AdjArgs& A, int64_t p, const PrepFP64& q, int
   const float fx = (float)(q.x - (double)q.lo[0]), fy = (float)(q.y - (double)q.lo[1]);
   const float fz = DIMS == 3 ? (float)(q.z - (double)q.lo[2]) : 0.0f;
   const float h = (float)q.hsml, hinv = 1.0f / h;
-  double qd[kAdjQ32];
-  for (int k = 0; k < kAdjQ32; ++k)
-    qd[k] = (k < nq && !q.scalar_zero) ? ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) : 0.0;
+  float qh[kAdjQ32], ql[kAdjQ32];  // q_k as FP32 (hi, lo)
+  for (int k = 0; k < kAdjQ32; ++k) {
+    const double v = (k < nq && !q.scalar_zero) ? ld_elem(pt.attr_dtype, pt.q, p * pt.qsp + k * pt.qsk) : 0.0;
+    qh[k] = (float)v;
+    ql[k] = (float)(v - (double)qh[k]);
+  }
   const int64_t P = A.mp.P;
   const int64_t i0 = q.lo[0], j0 = q.lo[1], k0 = q.lo[2];
-  // the image gradient at a footprint pixel, formed in FP64 (its parts
-  // cancel where q is near the map value) and rounded once
-  auto gamma_at = [&](int64_t idx) {
-    double gm = A.gw[idx];
+  const float* gh = A.g32;
+  const float* gl = A.g32 + (int64_t)(nq + 1) * A.PD;
+  // the image gradient at a footprint pixel (see kGamEps), rounded once;
+  // mag: |dL/dW| + sum_k |q_k dL/dQ_k|, the scale of its formation error
+  auto gamma_at = [&](int64_t idx, float& mag) {
+    float s = gh[(int64_t)nq * A.PD + idx], e = gl[(int64_t)nq * A.PD + idx];
+    mag = fabsf(s);
     for (int k = 0; k < kAdjQ32; ++k) {
       if (k >= nq) break;
-      gm += qd[k] * A.gq[k * A.PD + idx];
+      const float gqh = gh[k * A.PD + idx], gql = gl[k * A.PD + idx];
+      const float pr = qh[k] * gqh, pe = fmaf(qh[k], gqh, -pr);  // qh gqh = pr + pe exactly
+      const float t = s + pr, bp = t - s, se = (s - (t - bp)) + (pr - bp);  // s + pr = t + se exactly
+      s = t;
+      e += (se + pe) + (qh[k] * gql + ql[k] * gqh);
+      mag += fabsf(pr);
     }
-    return (float)gm;
+    return s + e;
   };
   // pass 1: renormalisation sum, the smallest u (the forward's test) and
   // the weighted mean Gam1 of gam, which pass 2 subtracts from every term
@@ -479,7 +501,8 @@ __device__ int adj_fp32_sums(const AdjArgs& A, int64_t p, const PrepFP64& q, int
       const float g = kshape_f<KERN>(u) * (ox * oy * oz);
       comp_add(s1, c1, g);
       const int64_t idx = DIMS == 2 ? (i0 + a) * P + (j0 + b) : ((i0 + a) * P + (j0 + b)) * P + (k0 + c);
-      comp_add(sG1, cG1, gamma_at(idx) * g);
+      float mag;
+      comp_add(sG1, cG1, gamma_at(idx, mag) * g);
     }
   }
 #pragma unroll
@@ -523,12 +546,15 @@ __device__ int adj_fp32_sums(const AdjArgs& A, int64_t p, const PrepFP64& q, int
       const float eq = eps * g * gqk;
       bq[k] = fmaf(eq, eq, bq[k]);
     }
-    const float gam = gamma_at(idx), dgam = gam - Gam1;
+    float mag;
+    const float gam = gamma_at(idx, mag), dgam = gam - Gam1;
+    const float gerr = kGamEps * mag;  // gam's formation error
     comp_add(aS, cS, g);
     comp_add(aG, cG, gam * g);
-    bG = fmaf(eps * gam * g, eps * gam * g, bG);
+    const float tg = (eps * fabsf(gam) + gerr) * g;
+    bG = fmaf(tg, tg, bG);
     // squared error weight of a term (gam - Gam1) x
-    const float eg = eps * dgam;
+    const float eg = eps * fabsf(dgam) + gerr;
     const float w2 = eg * eg;
     for (int t = 0; t < 4; ++t) {
       comp_add(agd[t], cgd[t], dgam * dg[t]);
