@@ -232,9 +232,18 @@ constexpr int kAdjQ32 = 4;
 // own, and the sums again on its branch.
 constexpr double kSureU = 0.9999999;
 
+// A warp's per-axis terms of one footprint (shared memory): entry e < ni for
+// column i = iMin + e, then nj entries for the rows, then nk (3D); formed
+// once per footprint instead of once per cell, in the same FP64 operations.
+constexpr int kAxisTab = 256;
+struct AxisTab {
+  double dist[kAxisTab], ov[kAxisTab];
+  signed char dox[kAxisTab], doh[kAxisTab];
+};
+
 template <int DIMS, int KERN>
 __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
-                                  double& dK, double* dqk) {
+                                  double& dK, double* dqk, AxisTab* tab) {
   const unsigned full = 0xffffffffu;
   const DevParticles& pt = A.pt;
   const double L = A.mp.L;
@@ -245,6 +254,22 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
   const int64_t njk = nj * nk, F = ni * njk;
   const double xs[3] = {q.x, q.y, q.z};
   const double h = q.hsml, h_inv = q.h_inv;
+  const int64_t ntab = ni + nj + (DIMS == 3 ? nk : 0);
+  const bool use_tab = tab != nullptr && ntab <= kAxisTab;  // warp-uniform
+  if (use_tab) {
+    __syncwarp();  // the warp's previous footprint is read
+    for (int e = lane; e < ntab; e += 32) {
+      const int d = e < ni ? 0 : (e < ni + nj ? 1 : 2);
+      const double x = d == 0 ? q.x : (d == 1 ? q.y : q.z);
+      const int64_t c = d == 0 ? iMin + e : (d == 1 ? jMin + (e - ni) : kMin + (e - ni - nj));
+      cell_axis_fp64(x, h, c, &tab->dist[e], &tab->ov[e]);
+      const bool up = x + h < (double)(c + 1);
+      const bool dn = x - h > (double)c;
+      tab->dox[e] = (signed char)((up ? 1 : 0) - (dn ? 1 : 0));
+      tab->doh[e] = (signed char)((up ? 1 : 0) + (dn ? 1 : 0));
+    }
+    __syncwarp();
+  }
   double S, sgg, sgd[4], sd[4], sq[kMaxQ];
   bool fallback = false, decided = false;
   for (;;) {
@@ -257,11 +282,19 @@ __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q
       const int64_t cell[3] = {iMin + ia, jMin + jb, kMin + kc};
       double dist[3] = {0, 0, 0}, ov[3] = {1, 1, 1}, dox[3] = {0, 0, 0}, doh[3] = {0, 0, 0};
       for (int d = 0; d < DIMS; ++d) {
-        cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
-        const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
-        const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
-        dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
-        doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
+        if (use_tab) {
+          const int e = (int)(d == 0 ? ia : (d == 1 ? ni + jb : ni + nj + kc));
+          dist[d] = tab->dist[e];
+          ov[d] = tab->ov[e];
+          dox[d] = (double)tab->dox[e];
+          doh[d] = (double)tab->doh[e];
+        } else {
+          cell_axis_fp64(xs[d], h, cell[d], &dist[d], &ov[d]);
+          const bool up = xs[d] + h < (double)(cell[d] + 1);  // min() takes x + h
+          const bool dn = xs[d] - h > (double)cell[d];        // max() takes x - h
+          dox[d] = (up ? 1.0 : 0.0) - (dn ? 1.0 : 0.0);
+          doh[d] = (up ? 1.0 : 0.0) + (dn ? 1.0 : 0.0);
+        }
       }
       const double A_ = ov[0] * ov[1] * ov[2];
       double dA[4];
@@ -655,13 +688,15 @@ __global__ void __launch_bounds__(256, 2) k_adj_particles(AdjArgs A) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const DevParticles& pt = A.pt;
   const int nq = pt.nq;
+  __shared__ AxisTab tabs[8];
+  AxisTab* tab = &tabs[threadIdx.x >> 5];
   for (int64_t p = wid; p < pt.n; p += nw) {
     PrepFP64 q;
     const int state = prep_adj<DIMS>(pt, A.mp, p, lane, &q);
     double grad[4] = {0.0, 0.0, 0.0, 0.0};  // x, y, z, h (pixel units)
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
-    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
+    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk, tab);
     if (lane == 0) {
       float v[kAdjScales];
       write_outputs<DIMS>(A, p, state, q, grad, dK, dqk, v);
@@ -722,7 +757,7 @@ __global__ void __launch_bounds__(128, 4) k_adj_particles32(AdjArgs A) {
       } else {
         double grad[4] = {0.0, 0.0, 0.0, 0.0}, dK = 0.0, dqk[kMaxQ];
         for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
-        adj_particle_fp64<DIMS, KERN>(A, g0 + j, qj, lane, grad, dK, dqk);
+        adj_particle_fp64<DIMS, KERN>(A, g0 + j, qj, lane, grad, dK, dqk, nullptr);
         if (lane == j) {
           for (int t = 0; t < 4; ++t) gm[t] = grad[t];
           dKm = dK;
@@ -762,6 +797,8 @@ __global__ void __launch_bounds__(256, 2) k_adj_pending(AdjArgs A) {
   const int64_t np = (int64_t)*A.n_pend;
   float sc[kAdjScales];
   for (int c = 0; c < kAdjScales; ++c) sc[c] = 1e-3f * __uint_as_float(A.scale[c]);
+  __shared__ AxisTab tabs[8];
+  AxisTab* tab = &tabs[threadIdx.x >> 5];
   for (int64_t i = wid; i < np; i += nw) {
     const AdjPending e = A.pend[i];
     const int64_t p = e.p;
@@ -786,7 +823,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_pending(AdjArgs A) {
     double grad[4] = {0.0, 0.0, 0.0, 0.0};
     double dK = 0.0, dqk[kMaxQ];
     for (int k = 0; k < nq; ++k) dqk[k] = 0.0;
-    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk);
+    if (state == kPrepMapped) adj_particle_fp64<DIMS, KERN>(A, p, q, lane, grad, dK, dqk, tab);
     if (lane == 0) {
       float v[kAdjScales];
       write_outputs<DIMS>(A, p, state, q, grad, dK, dqk, v);
