@@ -218,18 +218,7 @@ struct AdjArgs {
 // Maps of at most this many quantities take the FP32 path.
 constexpr int kAdjQ32 = 4;
 
-// One mapped particle in FP64 (the warp's lanes stride over its footprint):
-// grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.  u is the forward's
-// to a few ulp (cell_fp64 forms sqrt(r^2) * (1/h)); a cell it moves across
-// u = 1 has a weight and a derivative of order (1 - u)^2 or less, nil.  The
-// forward's branch -- the fallback g = A where its renormalisation sum is
-// zero -- is settled inside the pass that gathers the sums: a cell with
-// u < kSureU (so the forward's u < 1) at positive overlap has a positive
-// term (every kernel shape is positive below u = 1, at least (2^-53)^10
-// there), and with no negative overlap in the footprint the sum is then
-// positive.  Only a
-// particle without such a cell (sub-pixel ones) runs the sum as a pass of its
-// own, and the sums again on its branch.
+// Below this u (within a few ulp of the forward's) the forward's u is < 1.
 constexpr double kSureU = 0.9999999;
 
 // A warp's per-axis terms of one footprint (shared memory): entry e < ni for
@@ -241,6 +230,19 @@ struct AxisTab {
   signed char dox[kAxisTab], doh[kAxisTab];
 };
 
+// One mapped particle in FP64 (the warp's lanes stride over its footprint):
+// grad (x, y, z, h in pixel units), dL/dK and dL/dq_k.  u is the forward's
+// to a few ulp (cell_fp64 forms sqrt(r^2) * (1/h)); a cell it moves across
+// u = 1 has a weight and a derivative of order (1 - u)^2 or less, nil.  The
+// forward's branch -- the fallback g = A where its renormalisation sum is
+// zero -- is settled inside the pass that gathers the sums: a cell with
+// u < kSureU at positive overlap has a positive term (every kernel shape is
+// positive below u = 1, at least (2^-53)^10 there), and with no negative
+// overlap in the footprint the sum is then positive.  Only a particle
+// without such a cell (sub-pixel ones) runs the sum as a pass of its own,
+// and the sums again on its branch.  tab: the warp's axis table, or NULL
+// (terms formed per cell, as for footprints of more than kAxisTab axis
+// entries).
 template <int DIMS, int KERN>
 __device__ void adj_particle_fp64(const AdjArgs& A, int64_t p, const PrepFP64& q, int lane, double grad[4],
                                   double& dK, double* dqk, AxisTab* tab) {
